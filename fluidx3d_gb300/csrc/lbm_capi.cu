@@ -1,0 +1,499 @@
+// C-ABI implementation (include/lbm_capi.h): owns the device buffers of one LBM domain, keeps the
+// time step and the lazy-update bookkeeping of the reference's LBM_Domain (src/lbm.cpp:96-332), and
+// launches the sm_103a kernels. No entry point exits the process or throws across the ABI.
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <new>
+#include "lbm_capi.h"
+#include "lbm_internal.h"
+
+using namespace fx3d;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(const int code, const char* fmt, ...) {
+	char buf[1024];
+	va_list ap;
+	va_start(ap, fmt);
+	std::vsnprintf(buf, sizeof(buf), fmt, ap);
+	va_end(ap);
+	g_last_error = buf;
+	return code;
+}
+int cuda_fail(const cudaError_t e, const char* what) {
+	return fail(e==cudaErrorMemoryAllocation ? LBM_ERR_OUT_OF_MEMORY : LBM_ERR_CUDA, "%s: %s (%s)", what, cudaGetErrorString(e), cudaGetErrorName(e));
+}
+#define FX3D_CUDA(call, what) do { const cudaError_t e_ = (call); if(e_!=cudaSuccess) return cuda_fail(e_, what); } while(0)
+
+// storage bytes of one DDF
+size_t ddf_bytes(const uint32_t storage) { return storage==LBM_FP32 ? 4u : 2u; }
+
+__global__ void k_fill_f32(float* p, const uint64_t n, const float v) {
+	for(uint64_t i=(uint64_t)blockIdx.x*blockDim.x+threadIdx.x; i<n; i+=(uint64_t)gridDim.x*blockDim.x) p[i] = v;
+}
+
+} // namespace
+
+struct lbm_domain {
+	lbm_config cfg;
+	Variant v;
+	GridDesc g;
+	float w;
+	int device;
+	cudaStream_t own_stream = nullptr, stream = nullptr;
+	void* fi = nullptr;
+	float* rho = nullptr;
+	float* u = nullptr;
+	uint8_t* flags = nullptr;
+	float* F = nullptr;
+	double* partials = nullptr; // REDUCE_BLOCKS*4 doubles of reduction scratch
+	double* sum_dev = nullptr;  // 4 doubles
+	double* sum_host = nullptr; // pinned, 4 doubles
+	uint64_t t = 0ull;
+	uint64_t t_last_update_fields = UINT64_MAX;
+	uint64_t t_last_force_field = UINT64_MAX;
+	bool initialized = false;
+
+	StepArgs args() const {
+		StepArgs a;
+		a.g = g; a.fi = fi; a.rho = rho; a.u = u; a.flags = flags; a.F = F;
+		a.t = t; a.fx = cfg.fx; a.fy = cfg.fy; a.fz = cfg.fz; a.w = w;
+		return a;
+	}
+	size_t field_bytes(const int field) const {
+		switch(field) {
+			case LBM_FIELD_RHO: return g.N*4u;
+			case LBM_FIELD_U: return g.N*12u;
+			case LBM_FIELD_FLAGS: return g.N;
+			case LBM_FIELD_F: return g.N*12u;
+			case LBM_FIELD_FI: return g.N*(size_t)cfg.velocity_set*ddf_bytes(cfg.storage);
+			default: return 0u;
+		}
+	}
+	void* field_ptr(const int field) const {
+		switch(field) {
+			case LBM_FIELD_RHO: return rho;
+			case LBM_FIELD_U: return u;
+			case LBM_FIELD_FLAGS: return flags;
+			case LBM_FIELD_F: return F;
+			case LBM_FIELD_FI: return fi;
+			default: return nullptr;
+		}
+	}
+};
+
+namespace {
+
+// make the domain's device current for this call (the caller's current device is restored)
+struct DeviceGuard {
+	int prev = -1;
+	bool changed = false;
+	cudaError_t err = cudaSuccess;
+	explicit DeviceGuard(const int dev) {
+		err = cudaGetDevice(&prev);
+		if(err==cudaSuccess && prev!=dev) { err = cudaSetDevice(dev); changed = err==cudaSuccess; }
+	}
+	~DeviceGuard() { if(changed) cudaSetDevice(prev); }
+};
+#define FX3D_DOMAIN(d) \
+	if(!(d)) return fail(LBM_ERR_INVALID_ARGUMENT, "%s: domain is NULL", __func__); \
+	DeviceGuard guard_((d)->device); \
+	if(guard_.err!=cudaSuccess) return cuda_fail(guard_.err, "cudaSetDevice");
+
+int launch_result(const cudaError_t e, const char* what) { return e==cudaSuccess ? LBM_OK : cuda_fail(e, what); }
+
+int ensure_F(lbm_domain* d) {
+	if(d->F) return LBM_OK;
+	FX3D_CUDA(cudaMalloc(&d->F, d->g.N*12u), "cudaMalloc(F)");
+	FX3D_CUDA(cudaMemsetAsync(d->F, 0, d->g.N*12u, d->stream), "cudaMemsetAsync(F)");
+	return LBM_OK;
+}
+
+int do_update_fields(lbm_domain* d) {
+	if(d->t==d->t_last_update_fields) return LBM_OK;
+	const StepArgs a = d->args();
+	cudaError_t e;
+	switch(d->v.storage) {
+		case ST_FP32: e = launch_update_fields_fp32(d->v, a, d->stream); break;
+		case ST_FP16S: e = launch_update_fields_fp16s(d->v, a, d->stream); break;
+		default: e = launch_update_fields_fp16c(d->v, a, d->stream); break;
+	}
+	if(e!=cudaSuccess) return cuda_fail(e, "update_fields");
+	d->t_last_update_fields = d->t;
+	return LBM_OK;
+}
+
+int do_update_force_field(lbm_domain* d) {
+	const int r = ensure_F(d);
+	if(r!=LBM_OK) return r;
+	if(d->t==d->t_last_force_field) return LBM_OK;
+	const StepArgs a = d->args();
+	cudaError_t e;
+	switch(d->v.storage) {
+		case ST_FP32: e = launch_update_force_field_fp32(d->v, a, d->F, d->stream); break;
+		case ST_FP16S: e = launch_update_force_field_fp16s(d->v, a, d->F, d->stream); break;
+		default: e = launch_update_force_field_fp16c(d->v, a, d->F, d->stream); break;
+	}
+	if(e!=cudaSuccess) return cuda_fail(e, "update_force_field");
+	d->t_last_force_field = d->t;
+	return LBM_OK;
+}
+
+int object_sum(lbm_domain* d, const int kind, const uint8_t marker, const double cx, const double cy, const double cz, double* out, const int nout) {
+	if(kind>0) {
+		const int r = do_update_force_field(d);
+		if(r!=LBM_OK) return r;
+	}
+	const float* F = kind>0 ? d->F : nullptr;
+	FX3D_CUDA(launch_object_sum(d->g, F, d->flags, marker, kind, cx, cy, cz, d->partials, d->sum_dev, d->stream), "object_sum");
+	FX3D_CUDA(cudaMemcpyAsync(d->sum_host, d->sum_dev, 4u*sizeof(double), cudaMemcpyDeviceToHost, d->stream), "cudaMemcpyAsync(object_sum)");
+	FX3D_CUDA(cudaStreamSynchronize(d->stream), "cudaStreamSynchronize");
+	for(int i=0; i<nout; i++) out[i] = d->sum_host[i];
+	return LBM_OK;
+}
+
+void release(lbm_domain* d) {
+	if(d->fi) cudaFree(d->fi);
+	if(d->rho) cudaFree(d->rho);
+	if(d->u) cudaFree(d->u);
+	if(d->flags) cudaFree(d->flags);
+	if(d->F) cudaFree(d->F);
+	if(d->partials) cudaFree(d->partials);
+	if(d->sum_dev) cudaFree(d->sum_dev);
+	if(d->sum_host) cudaFreeHost(d->sum_host);
+	if(d->own_stream) cudaStreamDestroy(d->own_stream);
+}
+
+} // namespace
+
+extern "C" {
+
+const char* lbm_last_error(void) { return g_last_error.c_str(); }
+
+int lbm_host_alloc(const size_t bytes, void** host_ptr) {
+	if(!host_ptr) return fail(LBM_ERR_INVALID_ARGUMENT, "lbm_host_alloc: NULL output");
+	*host_ptr = nullptr;
+	if(bytes==0u) return LBM_OK;
+	FX3D_CUDA(cudaHostAlloc(host_ptr, bytes, cudaHostAllocPortable), "cudaHostAlloc");
+	return LBM_OK;
+}
+int lbm_host_free(void* host_ptr) {
+	if(host_ptr) FX3D_CUDA(cudaFreeHost(host_ptr), "cudaFreeHost");
+	return LBM_OK;
+}
+
+float lbm_relaxation_rate(const float nu) {
+	const float tau = 3.0f*nu+0.5f; // LBM::get_tau (src/lbm.hpp:462)
+	char buf[64];
+	std::snprintf(buf, sizeof(buf), "%f", (double)(1.0f/tau)); // std::to_string(float) of src/lbm.cpp:374
+	return std::strtof(buf, nullptr);
+}
+
+uint32_t lbm_bytes_per_cell_device(const lbm_config* c) {
+	if(!c) return 0u;
+	uint32_t b = c->velocity_set*(uint32_t)ddf_bytes(c->storage)+17u;
+	if(c->extensions&LBM_EXT_FORCE_FIELD) b += 12u;
+	return b;
+}
+uint32_t lbm_bandwidth_bytes_per_cell(const lbm_config* c) {
+	if(!c) return 0u;
+	uint32_t b = c->velocity_set*2u*(uint32_t)ddf_bytes(c->storage)+1u;
+	if(c->extensions&LBM_EXT_FORCE_FIELD) b += 12u;
+	return b;
+}
+
+int lbm_domain_create(const lbm_config* c, lbm_domain** out) {
+	if(!c||!out) return fail(LBM_ERR_INVALID_ARGUMENT, "lbm_domain_create: NULL argument");
+	*out = nullptr;
+	const uint64_t N = (uint64_t)c->Nx*c->Ny*c->Nz;
+	if(N==0ull) return fail(LBM_ERR_INVALID_ARGUMENT, "Grid point number is 0: %ux%ux%u = 0.", c->Nx, c->Ny, c->Nz);
+	if(c->Nz>65535u) return fail(LBM_ERR_INVALID_ARGUMENT, "Nz=%u exceeds 65535 (one launch row of planes per z)", c->Nz);
+	if((uint64_t)c->Nx*c->Ny>0xFFFFFFFFull) return fail(LBM_ERR_INVALID_ARGUMENT, "Nx*Ny must fit in 32 bits");
+	if(c->velocity_set!=19u&&c->velocity_set!=27u) return fail(LBM_ERR_INVALID_ARGUMENT, "velocity_set must be 19 or 27, got %u", c->velocity_set);
+	if(c->collision>LBM_TRT) return fail(LBM_ERR_INVALID_ARGUMENT, "collision must be LBM_SRT or LBM_TRT");
+	if(c->storage>LBM_FP16C) return fail(LBM_ERR_INVALID_ARGUMENT, "storage must be LBM_FP32, LBM_FP16S or LBM_FP16C");
+	if(c->extensions&~7u) return fail(LBM_ERR_INVALID_ARGUMENT, "unknown extension bits 0x%x", c->extensions&~7u);
+	if(!(c->nu>0.0f)) return fail(LBM_ERR_INVALID_ARGUMENT, c->nu==0.0f ? "Viscosity cannot be 0." : "Viscosity cannot be negative.");
+	if(!(c->extensions&LBM_EXT_VOLUME_FORCE)&&(c->fx!=0.0f||c->fy!=0.0f||c->fz!=0.0f))
+		return fail(LBM_ERR_INVALID_ARGUMENT, "Volume force is set, but LBM_EXT_VOLUME_FORCE is not enabled.");
+	int ndev = 0;
+	if(cudaGetDeviceCount(&ndev)!=cudaSuccess||ndev==0) { cudaGetLastError(); return fail(LBM_ERR_NO_DEVICE, "no CUDA device available"); }
+	int dev = c->device;
+	if(dev<0) { if(cudaGetDevice(&dev)!=cudaSuccess) return fail(LBM_ERR_NO_DEVICE, "cudaGetDevice failed"); }
+	if(dev>=ndev) return fail(LBM_ERR_INVALID_ARGUMENT, "device %d does not exist (%d devices)", dev, ndev);
+	DeviceGuard guard(dev);
+	if(guard.err!=cudaSuccess) return cuda_fail(guard.err, "cudaSetDevice");
+
+	const size_t need = (size_t)N*lbm_bytes_per_cell_device(c);
+	size_t free_b = 0u, total_b = 0u;
+	FX3D_CUDA(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo");
+	if(need>free_b) return fail(LBM_ERR_OUT_OF_MEMORY, "Grid resolution (%u, %u, %u) is too large: %zu MB required, %zu MB available.",
+	                            c->Nx, c->Ny, c->Nz, need/1048576u, free_b/1048576u);
+
+	lbm_domain* d = new(std::nothrow) lbm_domain();
+	if(!d) return fail(LBM_ERR_OUT_OF_MEMORY, "host allocation failed");
+	d->cfg = *c;
+	d->device = dev;
+	d->v.q = (int)c->velocity_set;
+	d->v.trt = c->collision==LBM_TRT;
+	d->v.storage = (int)c->storage;
+	int ext = 0;
+	if(c->extensions&LBM_EXT_VOLUME_FORCE) ext |= EXT_VF;
+	if((c->extensions&LBM_EXT_FORCE_FIELD)&&(c->extensions&LBM_EXT_VOLUME_FORCE)) ext |= EXT_FF; // F acts on the fluid only with VOLUME_FORCE
+	if(c->extensions&LBM_EXT_EQUILIBRIUM_BOUNDARIES) ext |= EXT_EQ;
+	d->v.ext = ext;
+	d->g.Nx = c->Nx; d->g.Ny = c->Ny; d->g.Nz = c->Nz; d->g.NxNy = c->Nx*c->Ny; d->g.N = N;
+	d->g.nx_inv = c->Nx==1u ? 0ull : (~0ull)/c->Nx+1ull; // ceil(2^64/Nx)
+	d->w = lbm_relaxation_rate(c->nu);
+
+	cudaError_t e = cudaStreamCreateWithFlags(&d->own_stream, cudaStreamNonBlocking);
+	if(e==cudaSuccess) { d->stream = d->own_stream; e = cudaMalloc(&d->fi, d->field_bytes(LBM_FIELD_FI)); }
+	if(e==cudaSuccess) e = cudaMalloc(&d->rho, N*4u);
+	if(e==cudaSuccess) e = cudaMalloc(&d->u, N*12u);
+	if(e==cudaSuccess) e = cudaMalloc(&d->flags, N);
+	if(e==cudaSuccess && (c->extensions&LBM_EXT_FORCE_FIELD)) e = cudaMalloc(&d->F, N*12u);
+	if(e==cudaSuccess) e = cudaMalloc(&d->partials, (size_t)REDUCE_BLOCKS*4u*sizeof(double));
+	if(e==cudaSuccess) e = cudaMalloc(&d->sum_dev, 4u*sizeof(double));
+	if(e==cudaSuccess) e = cudaMallocHost(&d->sum_host, 4u*sizeof(double));
+	if(e==cudaSuccess) e = cudaMemsetAsync(d->fi, 0, d->field_bytes(LBM_FIELD_FI), d->stream);
+	if(e==cudaSuccess) { k_fill_f32<<<1024, 256, 0, d->stream>>>(d->rho, N, 1.0f); e = cudaGetLastError(); } // rho = 1 (src/lbm.cpp:124)
+	if(e==cudaSuccess) e = cudaMemsetAsync(d->u, 0, N*12u, d->stream);
+	if(e==cudaSuccess) e = cudaMemsetAsync(d->flags, 0, N, d->stream);
+	if(e==cudaSuccess && d->F) e = cudaMemsetAsync(d->F, 0, N*12u, d->stream);
+	if(e==cudaSuccess) e = cudaStreamSynchronize(d->stream);
+	if(e!=cudaSuccess) {
+		const int r = cuda_fail(e, "lbm_domain_create");
+		release(d);
+		delete d;
+		return r;
+	}
+	*out = d;
+	return LBM_OK;
+}
+
+int lbm_domain_destroy(lbm_domain* d) {
+	if(!d) return LBM_OK;
+	{
+		DeviceGuard guard(d->device);
+		if(d->stream) cudaStreamSynchronize(d->stream);
+		release(d);
+	}
+	delete d;
+	return LBM_OK;
+}
+
+int lbm_set_stream(lbm_domain* d, void* s) {
+	FX3D_DOMAIN(d);
+	d->stream = s ? (cudaStream_t)s : d->own_stream;
+	return LBM_OK;
+}
+int lbm_get_stream(lbm_domain* d, void** s) {
+	FX3D_DOMAIN(d);
+	if(!s) return fail(LBM_ERR_INVALID_ARGUMENT, "lbm_get_stream: NULL output");
+	*s = (void*)d->stream;
+	return LBM_OK;
+}
+int lbm_synchronize(lbm_domain* d) {
+	FX3D_DOMAIN(d);
+	FX3D_CUDA(cudaStreamSynchronize(d->stream), "cudaStreamSynchronize");
+	return LBM_OK;
+}
+
+int lbm_write_field(lbm_domain* d, const int field, const void* host, const size_t bytes) {
+	FX3D_DOMAIN(d);
+	if(field<LBM_FIELD_RHO||field>LBM_FIELD_FI) return fail(LBM_ERR_INVALID_ARGUMENT, "unknown field %d", field);
+	if(field==LBM_FIELD_F) { const int r = ensure_F(d); if(r!=LBM_OK) return r; }
+	if(!host) return fail(LBM_ERR_INVALID_ARGUMENT, "lbm_write_field: NULL host pointer");
+	if(bytes!=d->field_bytes(field)) return fail(LBM_ERR_INVALID_ARGUMENT, "lbm_write_field: %zu bytes given, field has %zu", bytes, d->field_bytes(field));
+	FX3D_CUDA(cudaMemcpyAsync(d->field_ptr(field), host, bytes, cudaMemcpyHostToDevice, d->stream), "cudaMemcpyAsync(write_field)");
+	FX3D_CUDA(cudaStreamSynchronize(d->stream), "cudaStreamSynchronize");
+	if(field==LBM_FIELD_FI) { d->t_last_update_fields = UINT64_MAX; d->t_last_force_field = UINT64_MAX; }
+	return LBM_OK;
+}
+
+int lbm_read_field(lbm_domain* d, const int field, void* host, const size_t bytes) {
+	FX3D_DOMAIN(d);
+	if(field<LBM_FIELD_RHO||field>LBM_FIELD_FI) return fail(LBM_ERR_INVALID_ARGUMENT, "unknown field %d", field);
+	if(field==LBM_FIELD_F && !d->F) return fail(LBM_ERR_UNSUPPORTED, "F does not exist: enable LBM_EXT_FORCE_FIELD or call lbm_update_force_field");
+	if(!host) return fail(LBM_ERR_INVALID_ARGUMENT, "lbm_read_field: NULL host pointer");
+	if(bytes!=d->field_bytes(field)) return fail(LBM_ERR_INVALID_ARGUMENT, "lbm_read_field: %zu bytes given, field has %zu", bytes, d->field_bytes(field));
+	if(d->initialized && (field==LBM_FIELD_RHO||field==LBM_FIELD_U)) { const int r = do_update_fields(d); if(r!=LBM_OK) return r; }
+	FX3D_CUDA(cudaMemcpyAsync(host, d->field_ptr(field), bytes, cudaMemcpyDeviceToHost, d->stream), "cudaMemcpyAsync(read_field)");
+	FX3D_CUDA(cudaStreamSynchronize(d->stream), "cudaStreamSynchronize");
+	return LBM_OK;
+}
+
+int lbm_field_device_pointer(lbm_domain* d, const int field, void** ptr, size_t* bytes) {
+	FX3D_DOMAIN(d);
+	if(field<LBM_FIELD_RHO||field>LBM_FIELD_FI) return fail(LBM_ERR_INVALID_ARGUMENT, "unknown field %d", field);
+	if(field==LBM_FIELD_F) { const int r = ensure_F(d); if(r!=LBM_OK) return r; }
+	if(ptr) *ptr = d->field_ptr(field);
+	if(bytes) *bytes = d->field_bytes(field);
+	return LBM_OK;
+}
+
+int lbm_initialize(lbm_domain* d) {
+	FX3D_DOMAIN(d);
+	d->t = 1ull; // the initialize kernel stores at odd parity (src/lbm.cpp:904)
+	const StepArgs a = d->args();
+	cudaError_t e;
+	switch(d->v.storage) {
+		case ST_FP32: e = launch_initialize_fp32(d->v, a, d->stream); break;
+		case ST_FP16S: e = launch_initialize_fp16s(d->v, a, d->stream); break;
+		default: e = launch_initialize_fp16c(d->v, a, d->stream); break;
+	}
+	d->t = 0ull; // src/lbm.cpp:920
+	if(e!=cudaSuccess) return cuda_fail(e, "initialize");
+	d->t_last_update_fields = UINT64_MAX;
+	d->t_last_force_field = UINT64_MAX;
+	d->initialized = true;
+	return LBM_OK;
+}
+
+int lbm_stream_collide(lbm_domain* d, const uint64_t steps) {
+	FX3D_DOMAIN(d);
+	if(!d->initialized) return fail(LBM_ERR_NOT_INITIALIZED, "lbm_stream_collide: call lbm_initialize first");
+	for(uint64_t s=0ull; s<steps; s++) {
+		const StepArgs a = d->args();
+		cudaError_t e;
+		switch(d->v.storage) {
+			case ST_FP32: e = launch_stream_collide_fp32(d->v, a, d->stream); break;
+			case ST_FP16S: e = launch_stream_collide_fp16s(d->v, a, d->stream); break;
+			default: e = launch_stream_collide_fp16c(d->v, a, d->stream); break;
+		}
+		if(e!=cudaSuccess) return cuda_fail(e, "stream_collide");
+		d->t++;
+	}
+	return LBM_OK;
+}
+
+int lbm_update_fields(lbm_domain* d) {
+	FX3D_DOMAIN(d);
+	if(!d->initialized) return fail(LBM_ERR_NOT_INITIALIZED, "lbm_update_fields: call lbm_initialize first");
+	return do_update_fields(d);
+}
+
+int lbm_get_time_step(lbm_domain* d, uint64_t* t) {
+	if(!d||!t) return fail(LBM_ERR_INVALID_ARGUMENT, "lbm_get_time_step: NULL argument");
+	*t = d->t;
+	return LBM_OK;
+}
+int lbm_set_force(lbm_domain* d, const float fx, const float fy, const float fz) {
+	if(!d) return fail(LBM_ERR_INVALID_ARGUMENT, "lbm_set_force: domain is NULL");
+	if(!(d->cfg.extensions&LBM_EXT_VOLUME_FORCE)&&(fx!=0.0f||fy!=0.0f||fz!=0.0f))
+		return fail(LBM_ERR_UNSUPPORTED, "Volume force is set, but LBM_EXT_VOLUME_FORCE is not enabled.");
+	d->cfg.fx = fx; d->cfg.fy = fy; d->cfg.fz = fz;
+	d->t_last_update_fields = UINT64_MAX;
+	return LBM_OK;
+}
+int lbm_is_initialized(lbm_domain* d, int* initialized) {
+	if(!d||!initialized) return fail(LBM_ERR_INVALID_ARGUMENT, "lbm_is_initialized: NULL argument");
+	*initialized = d->initialized ? 1 : 0;
+	return LBM_OK;
+}
+int lbm_reset(lbm_domain* d) {
+	if(!d) return fail(LBM_ERR_INVALID_ARGUMENT, "lbm_reset: domain is NULL");
+	d->initialized = false;
+	return LBM_OK;
+}
+
+int lbm_update_force_field(lbm_domain* d) {
+	FX3D_DOMAIN(d);
+	if(!d->initialized) return fail(LBM_ERR_NOT_INITIALIZED, "lbm_update_force_field: call lbm_initialize first");
+	return do_update_force_field(d);
+}
+int lbm_reset_force_field(lbm_domain* d) {
+	FX3D_DOMAIN(d);
+	const int r = ensure_F(d);
+	if(r!=LBM_OK) return r;
+	FX3D_CUDA(cudaMemsetAsync(d->F, 0, d->g.N*12u, d->stream), "cudaMemsetAsync(F)");
+	d->t_last_force_field = UINT64_MAX;
+	return LBM_OK;
+}
+
+int lbm_object_center_of_mass(lbm_domain* d, const uint8_t marker, double out[4]) {
+	FX3D_DOMAIN(d);
+	if(!out) return fail(LBM_ERR_INVALID_ARGUMENT, "lbm_object_center_of_mass: NULL output");
+	double s[4];
+	const int r = object_sum(d, 0, marker, 0.0, 0.0, 0.0, s, 4);
+	if(r!=LBM_OK) return r;
+	out[3] = s[3];
+	for(int i=0; i<3; i++) out[i] = s[3]>0.0 ? s[i]/s[3] : 0.0;
+	return LBM_OK;
+}
+int lbm_object_force(lbm_domain* d, const uint8_t marker, double out[3]) {
+	FX3D_DOMAIN(d);
+	if(!out) return fail(LBM_ERR_INVALID_ARGUMENT, "lbm_object_force: NULL output");
+	if(!d->initialized) return fail(LBM_ERR_NOT_INITIALIZED, "lbm_object_force: call lbm_initialize first");
+	return object_sum(d, 1, marker, 0.0, 0.0, 0.0, out, 3);
+}
+int lbm_object_torque(lbm_domain* d, const uint8_t marker, const double cx, const double cy, const double cz, double out[3]) {
+	FX3D_DOMAIN(d);
+	if(!out) return fail(LBM_ERR_INVALID_ARGUMENT, "lbm_object_torque: NULL output");
+	if(!d->initialized) return fail(LBM_ERR_NOT_INITIALIZED, "lbm_object_torque: call lbm_initialize first");
+	return object_sum(d, 2, marker, cx, cy, cz, out, 3);
+}
+
+int lbm_voxelize_mesh(lbm_domain* d, const float* p0, const float* p1, const float* p2, const uint32_t T, const uint8_t flag,
+                      const float center[3], const float linear_velocity[3], const float rotational_velocity[3]) {
+	FX3D_DOMAIN(d);
+	if(T==0u) return LBM_OK;
+	if(!p0||!p1||!p2) return fail(LBM_ERR_INVALID_ARGUMENT, "lbm_voxelize_mesh: NULL vertex array");
+	const float zero[3] = {0.0f, 0.0f, 0.0f};
+	const float* c = center ? center : zero;
+	const float* lv = linear_velocity ? linear_velocity : zero;
+	const float* rv = rotational_velocity ? rotational_velocity : zero;
+	// mesh bounds (Mesh::find_bounds, src/utilities.hpp:4458-4469)
+	float pmin[3] = {p0[0], p0[1], p0[2]}, pmax[3] = {p0[0], p0[1], p0[2]};
+	for(uint32_t i=0u; i<T; i++) {
+		for(int k=0; k<3; k++) {
+			pmin[k] = fminf(fminf(fminf(p0[3u*i+k], p1[3u*i+k]), p2[3u*i+k]), pmin[k]);
+			pmax[k] = fmaxf(fmaxf(fmaxf(p0[3u*i+k], p1[3u*i+k]), p2[3u*i+k]), pmax[k]);
+		}
+	}
+	// bounding box +-2 cells, rotation centre and velocities (src/lbm.cpp:280-296)
+	float bbu[16];
+	std::memcpy(&bbu[0], &T, 4);
+	const float x0 = pmin[0]-2.0f, y0 = pmin[1]-2.0f, z0 = pmin[2]-2.0f, x1 = pmax[0]+2.0f, y1 = pmax[1]+2.0f, z1 = pmax[2]+2.0f;
+	bbu[1] = x0; bbu[2] = y0; bbu[3] = z0; bbu[4] = x1; bbu[5] = y1; bbu[6] = z1;
+	for(int k=0; k<3; k++) { bbu[7+k] = c[k]; bbu[10+k] = lv[k]; bbu[13+k] = rv[k]; }
+	// ray direction (src/lbm.cpp:297-318)
+	uint32_t direction = 0u;
+	if(sqrtf(rv[0]*rv[0]+rv[1]*rv[1]+rv[2]*rv[2])==0.0f) {
+		const float v[3] = {(y1-y0)*(z1-z0), (z1-z0)*(x1-x0), (x1-x0)*(y1-y0)};
+		float vmin = v[0];
+		for(uint32_t i=1u; i<3u; i++) if(v[i]<vmin) { vmin = v[i]; direction = i; }
+	} else {
+		const float v[3] = {fabsf(rv[0]), fabsf(rv[1]), fabsf(rv[2])};
+		float vmax = v[0];
+		for(uint32_t i=1u; i<3u; i++) if(v[i]>vmax) { vmax = v[i]; direction = i; }
+	}
+	float* dev = nullptr;
+	const size_t tb = (size_t)T*12u;
+	FX3D_CUDA(cudaMalloc(&dev, 3u*tb+16u*sizeof(float)), "cudaMalloc(mesh)");
+	cudaError_t e = cudaMemcpyAsync(dev, p0, tb, cudaMemcpyHostToDevice, d->stream);
+	if(e==cudaSuccess) e = cudaMemcpyAsync((char*)dev+tb, p1, tb, cudaMemcpyHostToDevice, d->stream);
+	if(e==cudaSuccess) e = cudaMemcpyAsync((char*)dev+2u*tb, p2, tb, cudaMemcpyHostToDevice, d->stream);
+	if(e==cudaSuccess) e = cudaMemcpyAsync((char*)dev+3u*tb, bbu, sizeof(bbu), cudaMemcpyHostToDevice, d->stream);
+	if(e==cudaSuccess) e = launch_voxelize(d->v, d->g, direction, d->fi, d->u, d->flags, d->t+1ull, flag,
+	                                       dev, (const float*)((char*)dev+tb), (const float*)((char*)dev+2u*tb), (const float*)((char*)dev+3u*tb), d->stream);
+	if(e==cudaSuccess) e = cudaStreamSynchronize(d->stream);
+	cudaFree(dev);
+	if(e!=cudaSuccess) return cuda_fail(e, "voxelize_mesh");
+	return LBM_OK;
+}
+
+int lbm_unvoxelize_mesh(lbm_domain* d, const float pmin[3], const float pmax[3], const uint8_t flag) {
+	FX3D_DOMAIN(d);
+	if(!pmin||!pmax) return fail(LBM_ERR_INVALID_ARGUMENT, "lbm_unvoxelize_mesh: NULL bounds");
+	const float box[6] = {pmin[0], pmin[1], pmin[2], pmax[0], pmax[1], pmax[2]};
+	FX3D_CUDA(launch_unvoxelize(d->g, d->flags, flag, box, d->stream), "unvoxelize_mesh");
+	return LBM_OK;
+}
+
+} // extern "C"

@@ -1,0 +1,102 @@
+// Storage-independent kernels: object reductions in FP64 and mesh unvoxelization.
+//
+//   k_object_sum + k_object_sum_final  src/kernel.cpp:1901-1959 object_center_of_mass/force/torque
+//   k_unvoxelize                       src/kernel.cpp:2359-2363 unvoxelize_mesh
+//
+// The reference reduces 64-cell work-groups in local memory and adds the group sums into 4 floats
+// with float atomics, so its result depends on scheduling. Here each of REDUCE_BLOCKS blocks
+// accumulates a fixed, strided subset of cells in FP64 (warp shuffles, then shared memory) into its
+// own slot of a partials buffer, and one block adds the partials in a fixed order: the sum is FP64
+// and bit-reproducible from run to run.
+#include "lbm_internal.h"
+#include "lbm_scheme.cuh"
+
+namespace fx3d {
+
+constexpr int RB = 256; // threads per reduction block
+
+__device__ __forceinline__ double warp_sum(double v) {
+	#pragma unroll
+	for(int o=16; o>0; o>>=1) v += __shfl_down_sync(0xFFFFFFFFu, v, o);
+	return v;
+}
+
+// block sum of 4 values into out[0..3] (thread 0 writes); fixed reduction order
+__device__ __forceinline__ void block_sum4(double v[4], double* out) {
+	__shared__ double sm[RB/32][4];
+	const int lane = threadIdx.x&31, warp = threadIdx.x>>5;
+	#pragma unroll
+	for(int k=0; k<4; k++) v[k] = warp_sum(v[k]);
+	if(lane==0) { for(int k=0; k<4; k++) sm[warp][k] = v[k]; }
+	__syncthreads();
+	if(warp==0) {
+		#pragma unroll
+		for(int k=0; k<4; k++) {
+			double s = lane<RB/32 ? sm[lane][k] : 0.0;
+			s = warp_sum(s);
+			if(lane==0) out[k] = s;
+		}
+	}
+}
+
+__global__ void __launch_bounds__(RB) k_object_sum(const GridDesc g, const float* __restrict__ F, const uint8_t* __restrict__ flags, const uint8_t marker,
+                                                   const int kind, const double cx, const double cy, const double cz, double* __restrict__ partials) {
+	double v[4] = {0.0, 0.0, 0.0, 0.0};
+	const uint64_t N = g.N, stride = (uint64_t)gridDim.x*RB;
+	for(uint64_t n=(uint64_t)blockIdx.x*RB+threadIdx.x; n<N; n+=stride) {
+		if(flags[n]!=marker) continue;
+		if(kind==1) { v[0] += (double)F[n]; v[1] += (double)F[N+n]; v[2] += (double)F[2ull*N+n]; continue; }
+		const uint64_t z = n/g.NxNy;
+		const uint32_t xy = (uint32_t)(n-z*g.NxNy);
+		const uint32_t y = xy/g.Nx, x = xy-y*g.Nx;
+		// cell position in box-centred coordinates, FP32 as the reference's position() (src/kernel.cpp:827-829)
+		const double px = (double)__fsub_rn(__fadd_rn((float)x, 0.5f), __fmul_rn(0.5f, (float)g.Nx));
+		const double py = (double)__fsub_rn(__fadd_rn((float)y, 0.5f), __fmul_rn(0.5f, (float)g.Ny));
+		const double pz = (double)__fsub_rn(__fadd_rn((float)z, 0.5f), __fmul_rn(0.5f, (float)g.Nz));
+		if(kind==0) { v[0] += px; v[1] += py; v[2] += pz; v[3] += 1.0; }
+		else {
+			const double Fx = F[n], Fy = F[N+n], Fz = F[2ull*N+n];
+			const double rx = px-cx, ry = py-cy, rz = pz-cz;
+			v[0] += ry*Fz-rz*Fy; v[1] += rz*Fx-rx*Fz; v[2] += rx*Fy-ry*Fx;
+		}
+	}
+	block_sum4(v, partials+4ull*blockIdx.x);
+}
+
+__global__ void __launch_bounds__(RB) k_object_sum_final(const double* __restrict__ partials, const int blocks, double* __restrict__ out) {
+	double v[4] = {0.0, 0.0, 0.0, 0.0};
+	for(int b=threadIdx.x; b<blocks; b+=RB) {
+		#pragma unroll
+		for(int k=0; k<4; k++) v[k] += partials[4*b+k];
+	}
+	block_sum4(v, out);
+}
+
+cudaError_t launch_object_sum(const GridDesc& g, const float* F, const uint8_t* flags, const uint8_t marker, const int kind,
+                              const double cx, const double cy, const double cz, double* partials, double* out, cudaStream_t s) {
+	k_object_sum<<<REDUCE_BLOCKS, RB, 0, s>>>(g, F, flags, marker, kind, cx, cy, cz, partials);
+	k_object_sum_final<<<1, RB, 0, s>>>(partials, REDUCE_BLOCKS, out);
+	return cudaGetLastError();
+}
+
+// box[6] = x0,y0,z0,x1,y1,z1 (mesh bounds); cells within +-1 lose `flag`
+__global__ void __launch_bounds__(BLOCK) k_unvoxelize(const GridDesc g, uint8_t* __restrict__ flags, const uint8_t flag,
+                                                      const float x0, const float y0, const float z0, const float x1, const float y1, const float z1) {
+	const uint32_t xy = blockIdx.x*(uint32_t)BLOCK+threadIdx.x;
+	if(xy>=g.NxNy) return;
+	const uint32_t z = blockIdx.y, y = xy/g.Nx, x = xy-y*g.Nx;
+	const uint64_t n = (uint64_t)z*g.NxNy+xy;
+	// position()+offset of src/kernel.cpp:2361 with zero domain offset
+	const float px = __fadd_rn(__fsub_rn(__fadd_rn((float)x, 0.5f), __fmul_rn(0.5f, (float)g.Nx)), __fsub_rn(__fmul_rn(0.5f, (float)(int)g.Nx), 0.5f));
+	const float py = __fadd_rn(__fsub_rn(__fadd_rn((float)y, 0.5f), __fmul_rn(0.5f, (float)g.Ny)), __fsub_rn(__fmul_rn(0.5f, (float)(int)g.Ny), 0.5f));
+	const float pz = __fadd_rn(__fsub_rn(__fadd_rn((float)z, 0.5f), __fmul_rn(0.5f, (float)g.Nz)), __fsub_rn(__fmul_rn(0.5f, (float)(int)g.Nz), 0.5f));
+	if(px>=x0-1.0f&&py>=y0-1.0f&&pz>=z0-1.0f&&px<=x1+1.0f&&py<=y1+1.0f&&pz<=z1+1.0f) flags[n] &= (uint8_t)~flag;
+}
+
+cudaError_t launch_unvoxelize(const GridDesc& g, uint8_t* flags, const uint8_t flag, const float* box, cudaStream_t s) {
+	const dim3 grid((g.NxNy+BLOCK-1u)/BLOCK, g.Nz, 1u);
+	k_unvoxelize<<<grid, BLOCK, 0, s>>>(g, flags, flag, box[0], box[1], box[2], box[3], box[4], box[5]);
+	return cudaGetLastError();
+}
+
+} // namespace fx3d

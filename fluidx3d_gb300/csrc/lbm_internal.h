@@ -1,0 +1,61 @@
+// Host-side declarations shared by the C-ABI (lbm_capi.cu) and the kernel translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace fx3d {
+
+enum : int { ST_FP32 = 0, ST_FP16S = 1, ST_FP16C = 2 }; // DDF storage formats
+enum : int { EXT_VF = 1, EXT_FF = 2, EXT_EQ = 4 };          // VOLUME_FORCE, FORCE_FIELD, EQUILIBRIUM_BOUNDARIES
+
+struct GridDesc { // mirrors fx3d::Grid of lbm_scheme.cuh (kept layout-identical)
+	uint32_t Nx, Ny, Nz, NxNy;
+	uint64_t N;
+	uint64_t nx_inv;
+};
+
+struct Variant {
+	int q;        // 19 or 27
+	bool trt;     // false: SRT
+	int storage;  // ST_FP32 / ST_FP16S / ST_FP16C
+	int ext;      // EXT_* bits, normalised: FF only together with VF
+};
+
+// arguments of one stream_collide / update_fields launch
+struct StepArgs {
+	GridDesc g;
+	void* fi;
+	float* rho;
+	float* u;
+	const uint8_t* flags;
+	const float* F;
+	uint64_t t;
+	float fx, fy, fz, w;
+};
+
+constexpr int BLOCK = 256;
+
+// per-storage launchers (lbm_kernels_<storage>.cu)
+#define FX3D_DECLARE_LAUNCHERS(sfx) \
+	cudaError_t launch_initialize_##sfx(const Variant& v, const StepArgs& a, cudaStream_t s); \
+	cudaError_t launch_stream_collide_##sfx(const Variant& v, const StepArgs& a, cudaStream_t s); \
+	cudaError_t launch_update_fields_##sfx(const Variant& v, const StepArgs& a, cudaStream_t s); \
+	cudaError_t launch_update_force_field_##sfx(const Variant& v, const StepArgs& a, float* F, cudaStream_t s);
+FX3D_DECLARE_LAUNCHERS(fp32)
+FX3D_DECLARE_LAUNCHERS(fp16s)
+FX3D_DECLARE_LAUNCHERS(fp16c)
+#undef FX3D_DECLARE_LAUNCHERS
+
+// storage-independent kernels (lbm_fields.cu)
+// kind 0: center-of-mass sums (x,y,z,count), 1: force, 2: torque about c; FP64 partial sums per
+// block into partials[blocks*4], then a fixed-order final sum into out[4] (deterministic)
+constexpr int REDUCE_BLOCKS = 608; // 4 blocks per SM on 152 SMs
+cudaError_t launch_object_sum(const GridDesc& g, const float* F, const uint8_t* flags, uint8_t marker, int kind,
+                              double cx, double cy, double cz, double* partials, double* out, cudaStream_t s);
+cudaError_t launch_unvoxelize(const GridDesc& g, uint8_t* flags, uint8_t flag, const float* box, cudaStream_t s);
+
+// voxelization (lbm_voxelize.cu); bbu: 16 floats in the reference's layout (src/lbm.cpp:280-296)
+cudaError_t launch_voxelize(const Variant& v, const GridDesc& g, uint32_t direction, void* fi, float* u, uint8_t* flags, uint64_t t, uint8_t flag,
+                            const float* p0, const float* p1, const float* p2, const float* bbu, cudaStream_t s);
+
+} // namespace fx3d

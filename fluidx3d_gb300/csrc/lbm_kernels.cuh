@@ -1,0 +1,191 @@
+// Per-cell LBM kernels (one thread per cell, plane-major launch: blockIdx.y = z, threads cover the
+// x-fastest cells of one plane) and their variant dispatch. Included once per DDF storage format by
+// lbm_kernels_<storage>.cu, so the three storage formats compile in parallel.
+//
+// Kernels and the reference functions they replace:
+//   k_initialize          src/kernel.cpp:1358-1430 initialize
+//   k_stream_collide      src/kernel.cpp:1454-1636 stream_collide
+//   k_update_fields       src/kernel.cpp:1794-1870 update_fields
+//   k_update_force_field  src/kernel.cpp:1873-1884 update_force_field
+#pragma once
+#include "lbm_scheme.cuh"
+#include "lbm_internal.h"
+
+namespace fx3d {
+
+static_assert(sizeof(GridDesc)==sizeof(Grid), "GridDesc must mirror Grid");
+__device__ __forceinline__ const Grid& grid_of(const GridDesc& g) { return reinterpret_cast<const Grid&>(g); }
+
+struct CellPos { uint32_t x, y, z; uint64_t n; };
+// cell of this thread; false for the idle tail threads of a plane
+__device__ __forceinline__ bool cell_of_thread(const Grid& g, CellPos& c) {
+	const uint32_t xy = blockIdx.x*(uint32_t)BLOCK+threadIdx.x;
+	if(xy>=g.NxNy) return false;
+	c.z = blockIdx.y;
+	c.y = div_nx(g, xy);
+	c.x = xy-c.y*g.Nx;
+	c.n = (uint64_t)c.z*g.NxNy+xy;
+	return true;
+}
+
+template<int Q, int ST> __global__ void __launch_bounds__(BLOCK) k_initialize(const StepArgs a) {
+	typedef typename Codec<ST>::T T;
+	const Grid& g = grid_of(a.g);
+	CellPos c;
+	if(!cell_of_thread(g, c)) return;
+	const uint64_t n = c.n, N = g.N;
+	float ux, uy, uz;
+	if((a.flags[n]&TYPE_BO)==TYPE_S) { // solid cells start at rest (src/kernel.cpp:1370-1373)
+		ux = uy = uz = 0.0f;
+		a.u[n] = 0.0f; a.u[N+n] = 0.0f; a.u[2ull*N+n] = 0.0f;
+	} else {
+		ux = a.u[n]; uy = a.u[N+n]; uz = a.u[2ull*N+n];
+	}
+	const EqState s = eq_state(a.rho[n], ux, uy, uz);
+	float f[Q];
+	f[0] = feq0<Q>(s);
+	Unroll<1, Q, 2>::run([&](auto ic) { constexpr int i = decltype(ic)::value; feq_pair<Q, i>(s, f[i], f[i+1]); });
+	const Nbr nb(g, c.x, c.y, c.z);
+	store_f<Q, ST>((T*)a.fi, N, n, nb, true, f); // odd parity (src/kernel.cpp:1429)
+}
+
+// density and velocity of one cell from its streamed DDFs (or the preset TYPE_E values), force
+// shifted and clamped exactly as stream_collide / update_fields do
+template<int Q, int EXT> __device__ __forceinline__ void cell_rho_u(const StepArgs& a, const uint64_t n, const float* f, const bool is_e,
+                                                                    float& rho, float& ux, float& uy, float& uz, float& fx, float& fy, float& fz) {
+	constexpr bool VF = (EXT&EXT_VF)!=0, FF = (EXT&EXT_FF)!=0;
+	const uint64_t N = a.g.N;
+	if(is_e) {
+		rho = a.rho[n]; ux = a.u[n]; uy = a.u[N+n]; uz = a.u[2ull*N+n];
+	} else {
+		float mx, my, mz;
+		moments<Q>(f, rho, mx, my, mz);
+		ux = __fdiv_rn(mx, rho); uy = __fdiv_rn(my, rho); uz = __fdiv_rn(mz, rho);
+	}
+	fx = a.fx; fy = a.fy; fz = a.fz;
+	if constexpr(FF) { fx = __fadd_rn(fx, a.F[n]); fy = __fadd_rn(fy, a.F[N+n]); fz = __fadd_rn(fz, a.F[2ull*N+n]); }
+	shift_clamp<VF>(ux, uy, uz, rho, fx, fy, fz);
+}
+
+template<int Q, int ST, bool TRT, int EXT> __global__ void __launch_bounds__(BLOCK) k_stream_collide(const StepArgs a) {
+	typedef typename Codec<ST>::T T;
+	constexpr bool VF = (EXT&EXT_VF)!=0, EQ = (EXT&EXT_EQ)!=0;
+	const Grid& g = grid_of(a.g);
+	CellPos c;
+	if(!cell_of_thread(g, c)) return;
+	const uint64_t n = c.n;
+	const uint8_t flagsn = a.flags[n];
+	const uint8_t flagsn_bo = flagsn&TYPE_BO;
+	if(flagsn_bo==TYPE_S||(flagsn&TYPE_SU)==TYPE_G) return; // solid or gas: nothing to do
+	const Nbr nb(g, c.x, c.y, c.z);
+	const bool odd = (a.t&1ull)!=0ull;
+	float f[Q];
+	load_f<Q, ST>((const T*)a.fi, g.N, n, nb, odd, f);
+	const bool is_e = EQ && flagsn_bo==TYPE_E;
+	float rho, ux, uy, uz, fx, fy, fz;
+	cell_rho_u<Q, EXT>(a, n, f, is_e, rho, ux, uy, uz, fx, fy, fz);
+	collide<Q, TRT, VF>(f, rho, ux, uy, uz, fx, fy, fz, is_e, a.w);
+	store_f<Q, ST>((T*)a.fi, g.N, n, nb, odd, f);
+}
+
+template<int Q, int ST, int EXT> __global__ void __launch_bounds__(BLOCK) k_update_fields(const StepArgs a) {
+	typedef typename Codec<ST>::T T;
+	constexpr bool EQ = (EXT&EXT_EQ)!=0;
+	const Grid& g = grid_of(a.g);
+	CellPos c;
+	if(!cell_of_thread(g, c)) return;
+	const uint64_t n = c.n, N = g.N;
+	const uint8_t flagsn = a.flags[n];
+	const uint8_t flagsn_bo = flagsn&TYPE_BO;
+	if(flagsn_bo==TYPE_S||(flagsn&TYPE_SU)==TYPE_G) return;
+	if(EQ && flagsn_bo==TYPE_E) return; // preset rho/u of TYPE_E cells are kept
+	const Nbr nb(g, c.x, c.y, c.z);
+	float f[Q];
+	load_f<Q, ST>((const T*)a.fi, N, n, nb, (a.t&1ull)!=0ull, f);
+	float rho, ux, uy, uz, fx, fy, fz;
+	cell_rho_u<Q, EXT&~EXT_EQ>(a, n, f, false, rho, ux, uy, uz, fx, fy, fz);
+	a.rho[n] = rho; a.u[n] = ux; a.u[N+n] = uy; a.u[2ull*N+n] = uz;
+}
+
+// momentum exchange on TYPE_S cells: F = 2*rho*(m/rho) (the reference reuses calculate_rho_u)
+template<int Q, int ST> __global__ void __launch_bounds__(BLOCK) k_update_force_field(const StepArgs a, float* F) {
+	typedef typename Codec<ST>::T T;
+	const Grid& g = grid_of(a.g);
+	CellPos c;
+	if(!cell_of_thread(g, c)) return;
+	const uint64_t n = c.n, N = g.N;
+	if((a.flags[n]&TYPE_BO)!=TYPE_S) return;
+	const Nbr nb(g, c.x, c.y, c.z);
+	float f[Q];
+	load_f<Q, ST>((const T*)a.fi, N, n, nb, (a.t&1ull)!=0ull, f);
+	float rho, mx, my, mz;
+	moments<Q>(f, rho, mx, my, mz);
+	const float s = __fmul_rn(2.0f, rho);
+	F[n] = __fmul_rn(s, __fdiv_rn(mx, rho)); F[N+n] = __fmul_rn(s, __fdiv_rn(my, rho)); F[2ull*N+n] = __fmul_rn(s, __fdiv_rn(mz, rho));
+}
+
+// ---------------------------------------------------------------- dispatch
+inline dim3 cell_grid(const GridDesc& g) { return dim3((g.NxNy+BLOCK-1u)/BLOCK, g.Nz, 1u); }
+
+template<int ST, int Q, bool TRT, int EXT> inline void sc_launch(const StepArgs& a, cudaStream_t s) {
+	k_stream_collide<Q, ST, TRT, EXT><<<cell_grid(a.g), BLOCK, 0, s>>>(a);
+}
+template<int ST, int Q, bool TRT> inline bool sc_ext(const int ext, const StepArgs& a, cudaStream_t s) {
+	switch(ext) {
+		case 0:                        sc_launch<ST, Q, TRT, 0>(a, s); return true;
+		case EXT_VF:                   sc_launch<ST, Q, TRT, EXT_VF>(a, s); return true;
+		case EXT_VF|EXT_FF:            sc_launch<ST, Q, TRT, EXT_VF|EXT_FF>(a, s); return true;
+		case EXT_EQ:                   sc_launch<ST, Q, TRT, EXT_EQ>(a, s); return true;
+		case EXT_EQ|EXT_VF:            sc_launch<ST, Q, TRT, EXT_EQ|EXT_VF>(a, s); return true;
+		case EXT_EQ|EXT_VF|EXT_FF:     sc_launch<ST, Q, TRT, EXT_EQ|EXT_VF|EXT_FF>(a, s); return true;
+		default: return false;
+	}
+}
+template<int ST> cudaError_t launch_stream_collide_t(const Variant& v, const StepArgs& a, cudaStream_t s) {
+	bool ok;
+	if(v.q==19) ok = v.trt ? sc_ext<ST, 19, true>(v.ext, a, s) : sc_ext<ST, 19, false>(v.ext, a, s);
+	else ok = v.trt ? sc_ext<ST, 27, true>(v.ext, a, s) : sc_ext<ST, 27, false>(v.ext, a, s);
+	return ok ? cudaGetLastError() : cudaErrorInvalidValue;
+}
+
+template<int ST, int Q, int EXT> inline void uf_launch(const StepArgs& a, cudaStream_t s) {
+	k_update_fields<Q, ST, EXT><<<cell_grid(a.g), BLOCK, 0, s>>>(a);
+}
+template<int ST, int Q> inline bool uf_ext(const int ext, const StepArgs& a, cudaStream_t s) {
+	switch(ext) {
+		case 0:                        uf_launch<ST, Q, 0>(a, s); return true;
+		case EXT_VF:                   uf_launch<ST, Q, EXT_VF>(a, s); return true;
+		case EXT_VF|EXT_FF:            uf_launch<ST, Q, EXT_VF|EXT_FF>(a, s); return true;
+		case EXT_EQ:                   uf_launch<ST, Q, EXT_EQ>(a, s); return true;
+		case EXT_EQ|EXT_VF:            uf_launch<ST, Q, EXT_EQ|EXT_VF>(a, s); return true;
+		case EXT_EQ|EXT_VF|EXT_FF:     uf_launch<ST, Q, EXT_EQ|EXT_VF|EXT_FF>(a, s); return true;
+		default: return false;
+	}
+}
+template<int ST> cudaError_t launch_update_fields_t(const Variant& v, const StepArgs& a, cudaStream_t s) {
+	const bool ok = v.q==19 ? uf_ext<ST, 19>(v.ext, a, s) : v.q==27 ? uf_ext<ST, 27>(v.ext, a, s) : false;
+	return ok ? cudaGetLastError() : cudaErrorInvalidValue;
+}
+
+template<int ST> cudaError_t launch_initialize_t(const Variant& v, const StepArgs& a, cudaStream_t s) {
+	if(v.q==19) k_initialize<19, ST><<<cell_grid(a.g), BLOCK, 0, s>>>(a);
+	else if(v.q==27) k_initialize<27, ST><<<cell_grid(a.g), BLOCK, 0, s>>>(a);
+	else return cudaErrorInvalidValue;
+	return cudaGetLastError();
+}
+template<int ST> cudaError_t launch_update_force_field_t(const Variant& v, const StepArgs& a, float* F, cudaStream_t s) {
+	if(v.q==19) k_update_force_field<19, ST><<<cell_grid(a.g), BLOCK, 0, s>>>(a, F);
+	else if(v.q==27) k_update_force_field<27, ST><<<cell_grid(a.g), BLOCK, 0, s>>>(a, F);
+	else return cudaErrorInvalidValue;
+	return cudaGetLastError();
+}
+
+} // namespace fx3d
+
+#define FX3D_DEFINE_LAUNCHERS(sfx, ST) \
+	namespace fx3d { \
+	cudaError_t launch_initialize_##sfx(const Variant& v, const StepArgs& a, cudaStream_t s) { return launch_initialize_t<ST>(v, a, s); } \
+	cudaError_t launch_stream_collide_##sfx(const Variant& v, const StepArgs& a, cudaStream_t s) { return launch_stream_collide_t<ST>(v, a, s); } \
+	cudaError_t launch_update_fields_##sfx(const Variant& v, const StepArgs& a, cudaStream_t s) { return launch_update_fields_t<ST>(v, a, s); } \
+	cudaError_t launch_update_force_field_##sfx(const Variant& v, const StepArgs& a, float* F, cudaStream_t s) { return launch_update_force_field_t<ST>(v, a, F, s); } \
+	}

@@ -1,0 +1,135 @@
+/* C-ABI of the GB300 LBM solver core: one LBM domain on one CUDA device.
+ *
+ * This is the boundary the reference's host code would bind in place of its OpenCL layer
+ * (src/opencl.hpp: Device, Memory<T>, Kernel) and the per-domain enqueue calls of LBM_Domain
+ * (src/lbm.hpp:94-120, src/lbm.cpp:96-332). Plain pointers and sizes only; every entry point
+ * returns an lbm_status and never exits the process (the reference prints and calls exit(1),
+ * src/utilities.hpp:4159-4166); lbm_last_error() gives the message of the last failure on the
+ * calling thread.
+ *
+ * Layout of every field is the reference's (src/kernel.cpp:820-826, 861-863, 960-967):
+ *   cell index n = x+(y+z*Ny)*Nx; rho float[N]; u float[3N] (SoA: ux, then uy, then uz);
+ *   flags uint8[N]; F float[3N] (SoA); DDFs fi[i*N+n] in the storage type of the variant.
+ * Flag bits are the reference's TYPE_* values (src/defines.hpp:53-60).
+ *
+ * Streams: all work is enqueued on the domain's stream (a stream the library creates, or the
+ * caller's via lbm_set_stream). Entry points that return host data synchronise that stream.
+ */
+#ifndef FX3D_LBM_CAPI_H
+#define FX3D_LBM_CAPI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LBM_CAPI_VERSION 1
+
+typedef struct lbm_domain lbm_domain; /* opaque: one LBM_Domain on one GPU */
+
+typedef enum lbm_status {
+	LBM_OK = 0,
+	LBM_ERR_INVALID_ARGUMENT = 1, /* bad size, pointer, enum or configuration */
+	LBM_ERR_OUT_OF_MEMORY = 2,    /* device allocation failed (src/opencl.hpp:375-387 checks the same) */
+	LBM_ERR_CUDA = 3,             /* a CUDA runtime call failed */
+	LBM_ERR_NOT_INITIALIZED = 4,  /* the call needs lbm_initialize first */
+	LBM_ERR_UNSUPPORTED = 5,      /* the variant lacks the extension the call needs */
+	LBM_ERR_NO_DEVICE = 6         /* no CUDA device (the reference exits in get_devices, src/opencl.hpp:222-252) */
+} lbm_status;
+
+/* variant selection: the reference's compile-time switches (src/defines.hpp:5-29) as runtime values */
+enum { LBM_SRT = 0, LBM_TRT = 1 };
+enum { LBM_FP32 = 0, LBM_FP16S = 1, LBM_FP16C = 2 };
+enum {
+	LBM_EXT_VOLUME_FORCE = 1,          /* VOLUME_FORCE: global force (fx,fy,fz), Guo forcing */
+	LBM_EXT_FORCE_FIELD = 2,           /* FORCE_FIELD: per-cell force F added to (fx,fy,fz) */
+	LBM_EXT_EQUILIBRIUM_BOUNDARIES = 4 /* EQUILIBRIUM_BOUNDARIES: TYPE_E cells held at their rho/u */
+};
+enum { LBM_FIELD_RHO = 0, LBM_FIELD_U = 1, LBM_FIELD_FLAGS = 2, LBM_FIELD_F = 3, LBM_FIELD_FI = 4 };
+enum { LBM_TYPE_S = 0x01, LBM_TYPE_E = 0x02, LBM_TYPE_T = 0x04, LBM_TYPE_F = 0x08,
+       LBM_TYPE_I = 0x10, LBM_TYPE_G = 0x20, LBM_TYPE_X = 0x40, LBM_TYPE_Y = 0x80 };
+
+typedef struct lbm_config {
+	uint32_t Nx, Ny, Nz;     /* lattice size; Nz <= 65535, N = Nx*Ny*Nz >= 1 */
+	uint32_t velocity_set;   /* 19 (D3Q19) or 27 (D3Q27) */
+	uint32_t collision;      /* LBM_SRT or LBM_TRT */
+	uint32_t storage;        /* LBM_FP32, LBM_FP16S or LBM_FP16C DDF storage; arithmetic is FP32 */
+	uint32_t extensions;     /* LBM_EXT_* bits */
+	int32_t device;          /* CUDA device ordinal; -1: the calling thread's current device */
+	float nu;                /* kinematic shear viscosity, > 0 */
+	float fx, fy, fz;        /* global volume force (needs LBM_EXT_VOLUME_FORCE when non-zero) */
+} lbm_config;
+
+/* ---- lifetime: replaces LBM_Domain::LBM_Domain + allocate (src/lbm.cpp:96-176) and the
+ *      constructor sanity checks (src/lbm.cpp:783-838). rho is filled with 1, u/flags/F with 0. */
+int lbm_domain_create(const lbm_config* config, lbm_domain** domain);
+int lbm_domain_destroy(lbm_domain* domain);
+
+/* relaxation rate the kernels use: 1/tau, tau = 3*nu+1/2, rounded the way the reference bakes it
+ * into its kernel source as a "%f" literal (src/lbm.cpp:374) */
+float lbm_relaxation_rate(float nu);
+/* bytes per cell: device allocation and per-time-step traffic (src/lbm.cpp:38-72) */
+uint32_t lbm_bytes_per_cell_device(const lbm_config* config);
+uint32_t lbm_bandwidth_bytes_per_cell(const lbm_config* config);
+
+/* ---- streams and synchronisation (src/opencl.hpp: Device::finish_queue) */
+int lbm_set_stream(lbm_domain* domain, void* cuda_stream); /* NULL: back to the domain's own stream */
+int lbm_get_stream(lbm_domain* domain, void** cuda_stream);
+int lbm_synchronize(lbm_domain* domain);
+
+/* ---- fields: Memory<T>::enqueue_write_to_device / enqueue_read_from_device (src/opencl.hpp:510-531).
+ * bytes must equal the field size. Reading rho/u first brings them up to date with lbm_update_fields
+ * when the domain is initialised, as Memory_Container::read_from_device does (src/lbm.hpp:390-396).
+ * LBM_FIELD_F exists with LBM_EXT_FORCE_FIELD, or after lbm_update_force_field. */
+int lbm_write_field(lbm_domain* domain, int field, const void* host, size_t bytes);
+int lbm_read_field(lbm_domain* domain, int field, void* host, size_t bytes);
+int lbm_field_device_pointer(lbm_domain* domain, int field, void** device_ptr, size_t* bytes);
+
+/* ---- time stepping */
+/* initialize kernel at odd parity, then t = 0 (src/lbm.cpp:881-922; src/kernel.cpp:1358-1430) */
+int lbm_initialize(lbm_domain* domain);
+/* `steps` LBM time steps, each one stream_collide launch and t += 1 (src/lbm.cpp:181-183, 924-975;
+ * src/kernel.cpp:1454-1636); no host synchronisation between steps */
+int lbm_stream_collide(lbm_domain* domain, uint64_t steps);
+/* rho/u from the DDFs at the current t, skipped if already current (src/lbm.cpp:184-191) */
+int lbm_update_fields(lbm_domain* domain);
+int lbm_get_time_step(lbm_domain* domain, uint64_t* t);
+int lbm_set_force(lbm_domain* domain, float fx, float fy, float fz); /* LBM::set_f (src/lbm.hpp:469-473) */
+int lbm_is_initialized(lbm_domain* domain, int* initialized);
+int lbm_reset(lbm_domain* domain); /* next lbm_initialize starts over (src/lbm.cpp:982-984) */
+
+/* ---- forces on solids (src/lbm.cpp:207-229, 991-1015; src/kernel.cpp:1873-1959) */
+/* F = momentum exchange on TYPE_S cells at the current t (skipped if already current) */
+int lbm_update_force_field(lbm_domain* domain);
+int lbm_reset_force_field(lbm_domain* domain);
+/* masked sums over cells with flags == marker, accumulated in FP64 on the device:
+ * center of mass: out[0..2] = mean cell position (box-centred coordinates), out[3] = cell count;
+ * force: out[0..2] = sum F; torque: out[0..2] = sum (p - c) x F */
+int lbm_object_center_of_mass(lbm_domain* domain, uint8_t marker, double out[4]);
+int lbm_object_force(lbm_domain* domain, uint8_t marker, double out[3]);
+int lbm_object_torque(lbm_domain* domain, uint8_t marker, double cx, double cy, double cz, double out[3]);
+
+/* ---- mesh voxelization (src/lbm.cpp:275-327, 1074-1093; src/kernel.cpp:2267-2363).
+ * p0/p1/p2: host arrays of `triangles` vertices, xyz interleaved (float3 p0[triangles]), in lattice
+ * coordinates; center / linear_velocity / rotational_velocity as in LBM::voxelize_mesh_on_device.
+ * Cells inside get flags = (flags & ~(TYPE_S|TYPE_E)) | flag. */
+int lbm_voxelize_mesh(lbm_domain* domain, const float* p0, const float* p1, const float* p2, uint32_t triangles, uint8_t flag,
+                      const float center[3], const float linear_velocity[3], const float rotational_velocity[3]);
+/* clears `flag` in the mesh bounding box +-1 cell */
+int lbm_unvoxelize_mesh(lbm_domain* domain, const float pmin[3], const float pmax[3], uint8_t flag);
+
+/* ---- page-locked host buffers for fast field transfers (the reference's Memory<T> host side,
+ *      src/opencl.hpp:342-440, is plain pageable memory) */
+int lbm_host_alloc(size_t bytes, void** host_ptr);
+int lbm_host_free(void* host_ptr);
+
+/* message of the last failed call on this thread ("" if none) */
+const char* lbm_last_error(void);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* FX3D_LBM_CAPI_H */

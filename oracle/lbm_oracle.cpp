@@ -1,0 +1,540 @@
+// CPU ORACLE for the LBM solver path: TEST INFRASTRUCTURE ONLY.
+//
+// Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load this library, and only as
+// the checker or the timed CPU baseline; the product (fluidx3d_gb300) never calls it.
+//
+// A restatement, in plain C++, of the reference's LBM scheme for one domain:
+//   velocity sets, neighbours        src/kernel.cpp:861-958
+//   calculate_f_eq                   src/kernel.cpp:1004-1061
+//   calculate_rho_u                  src/kernel.cpp:1063-1088
+//   calculate_forcing_terms          src/kernel.cpp:1091-1101
+//   load_f / store_f (Esoteric-Pull) src/kernel.cpp:1326-1339
+//   initialize                       src/kernel.cpp:1358-1430
+//   stream_collide (SRT/TRT, TYPE_S, TYPE_E, VOLUME_FORCE, FORCE_FIELD)  src/kernel.cpp:1454-1636
+//   update_fields                    src/kernel.cpp:1794-1870
+//   update_force_field               src/kernel.cpp:1873-1884
+//   object_center_of_mass/force/torque (sums done in FP64 here)  src/kernel.cpp:1901-1959
+//   voxelize_mesh / unvoxelize_mesh  src/kernel.cpp:2267-2363
+//   FP16S / FP16C codecs             src/lbm.cpp:411-414, src/kernel.cpp:848-859
+//   relaxation rate literal          src/lbm.cpp:374 (def_w printed with "%f")
+//
+// Two instantiations:
+//   * "f32": FP32 arithmetic in the reference's operation order, with fma() exactly where the
+//     reference writes fma() and no other contraction (compiled with -ffp-contract=off); DDFs stored
+//     as FP32, FP16S or FP16C. Pinned bit-exact against the reference's own kernel text compiled for
+//     the CPU (oracle/ref_harness), and the target the CUDA kernels are compared with.
+//   * "f64": the same scheme in FP64 arithmetic and FP64 DDF storage: the error baseline for the FP32,
+//     FP16S and FP16C runs.
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <thread>
+#include <vector>
+#include "half_ieee.h"
+
+typedef uint8_t u8;
+typedef uint16_t u16;
+typedef uint32_t u32;
+typedef uint64_t u64;
+
+enum { ST_FP32 = 0, ST_FP16S = 1, ST_FP16C = 2 };
+enum { EXT_VOLUME_FORCE = 1, EXT_FORCE_FIELD = 2, EXT_EQUILIBRIUM_BOUNDARIES = 4 };
+enum { T_S = 0x01, T_E = 0x02, T_BO = 0x03, T_MS = 0x03, T_G = 0x20, T_SU = 0x38, T_XY = 0xC0 };
+
+extern "C" struct OracleConfig {
+	u32 Nx, Ny, Nz;
+	u32 q;        // 19 or 27
+	u32 trt;      // 0: SRT, 1: TRT
+	u32 storage;  // ST_*
+	u32 ext;      // EXT_* bits
+	u32 threads;  // host threads for the per-cell loops
+	double w;     // relaxation rate as the kernel sees it
+};
+
+// ------------------------------------------------------------------ velocity sets (src/kernel.cpp:878-887)
+static const int C19[3][19] = {
+	{0, 1,-1, 0, 0, 0, 0, 1,-1, 1,-1, 0, 0, 1,-1, 1,-1, 0, 0},
+	{0, 0, 0, 1,-1, 0, 0, 1,-1, 0, 0, 1,-1,-1, 1, 0, 0, 1,-1},
+	{0, 0, 0, 0, 0, 1,-1, 0, 0, 1,-1, 1,-1, 0, 0,-1, 1,-1, 1}};
+static const int C27[3][27] = {
+	{0, 1,-1, 0, 0, 0, 0, 1,-1, 1,-1, 0, 0, 1,-1, 1,-1, 0, 0, 1,-1, 1,-1, 1,-1,-1, 1},
+	{0, 0, 0, 1,-1, 0, 0, 1,-1, 0, 0, 1,-1,-1, 1, 0, 0, 1,-1, 1,-1, 1,-1,-1, 1, 1,-1},
+	{0, 0, 0, 0, 0, 1,-1, 0, 0, 1,-1, 1,-1, 0, 0,-1, 1,-1, 1, 1,-1,-1, 1, 1,-1, 1,-1}};
+
+static inline int cq(const u32 q, const int d, const u32 i) { return q==19u ? C19[d][i] : C27[d][i]; }
+
+template<typename real> struct Weights { real w0, ws, we, wc; };
+template<typename real> static Weights<real> weights(const u32 q) { // weights as the reference's defines spell them
+	Weights<real> r;
+	if(q==19u) { r.w0 = (real)1/(real)3; r.ws = (real)1/(real)18; r.we = (real)1/(real)36; r.wc = (real)0; }
+	else { r.w0 = (real)1/(real)3.375; r.ws = (real)1/(real)13.5; r.we = (real)1/(real)54; r.wc = (real)1/(real)216; }
+	return r;
+}
+template<typename real> static inline real weight(const Weights<real>& W, const u32 i) { return i==0u ? W.w0 : i<7u ? W.ws : i<19u ? W.we : W.wc; }
+
+// ------------------------------------------------------------------ storage codecs
+static inline float fp16c_to_float(const u16 x) { // src/kernel.cpp:848-852
+	const u32 e = ((u32)x&0x7800u)>>11;
+	const u32 m = ((u32)x&0x07FFu)<<12;
+	const float mf = (float)m;
+	u32 mfb; std::memcpy(&mfb, &mf, 4);
+	const u32 v = mfb>>23;
+	const u32 r = (((u32)x&0x8000u)<<16) | (u32)(e!=0u)*((e+112u)<<23|m) | (u32)((e==0u)&(m!=0u))*((v-37u)<<23|((m<<(150u-v))&0x007FF000u));
+	float f; std::memcpy(&f, &r, 4);
+	return f;
+}
+static inline u16 float_to_fp16c(const float x) { // src/kernel.cpp:853-858
+	u32 xb; std::memcpy(&xb, &x, 4);
+	const u32 b = xb+0x00000800u;
+	const u32 e = (b&0x7F800000u)>>23;
+	const u32 m = b&0x007FFFFFu;
+	return (u16)((b&0x80000000u)>>16 | (u32)(e>112u)*((((e-112u)<<11)&0x7800u)|m>>12) | (u32)((e<113u)&(e>100u))*((((0x007FF800u+m)>>(124u-e))+1u)>>1));
+}
+
+template<typename real> struct Store;
+template<> struct Store<double> { // FP64 oracle: DDFs kept in FP64
+	static inline double load(const void* p, const u64 o, u32) { return ((const double*)p)[o]; }
+	static inline void store(void* p, const u64 o, const double x, u32) { ((double*)p)[o] = x; }
+};
+template<> struct Store<float> {
+	static inline float load(const void* p, const u64 o, const u32 st) {
+		if(st==ST_FP16S) return half_bits_to_float(((const u16*)p)[o])*3.0517578E-5f;
+		if(st==ST_FP16C) return fp16c_to_float(((const u16*)p)[o]);
+		return ((const float*)p)[o];
+	}
+	static inline void store(void* p, const u64 o, const float x, const u32 st) {
+		if(st==ST_FP16S) ((u16*)p)[o] = float_to_half_bits_rne(x*32768.0f);
+		else if(st==ST_FP16C) ((u16*)p)[o] = float_to_fp16c(x);
+		else ((float*)p)[o] = x;
+	}
+};
+
+// ------------------------------------------------------------------ lattice helpers
+struct Grid {
+	u32 Nx, Ny, Nz; u64 N;
+	explicit Grid(const OracleConfig* c) : Nx(c->Nx), Ny(c->Ny), Nz(c->Nz), N((u64)c->Nx*c->Ny*c->Nz) {}
+	inline void coords(const u64 n, u32& x, u32& y, u32& z) const {
+		const u64 t = n%((u64)Nx*Ny);
+		x = (u32)(t%Nx); y = (u32)(t/Nx); z = (u32)(n/((u64)Nx*Ny));
+	}
+	inline u64 index(const u32 x, const u32 y, const u32 z) const { return (u64)x+((u64)y+(u64)z*Ny)*(u64)Nx; }
+	// j[i] = periodic neighbour in direction c_i (src/kernel.cpp:904-958)
+	inline void neighbors(const u64 n, const u32 q, u64* j) const {
+		u32 x, y, z; coords(n, x, y, z);
+		j[0] = n;
+		for(u32 i=1u; i<q; i++) {
+			const u32 xi = (u32)(((int64_t)x+cq(q, 0, i)+Nx)%Nx);
+			const u32 yi = (u32)(((int64_t)y+cq(q, 1, i)+Ny)%Ny);
+			const u32 zi = (u32)(((int64_t)z+cq(q, 2, i)+Nz)%Nz);
+			j[i] = index(xi, yi, zi);
+		}
+	}
+};
+
+template<typename L> static void parallel_cells(const u64 items, const u32 threads, L&& body) {
+	const u32 T = threads>0u ? threads : 1u;
+	if(T==1u || items<4096ull) { for(u64 n=0ull; n<items; n++) body(n); return; }
+	std::vector<std::thread> pool;
+	for(u32 t=0u; t<T; t++) pool.emplace_back([=, &body]() { for(u64 n=items*t/T; n<items*(t+1u)/T; n++) body(n); });
+	for(auto& th : pool) th.join();
+}
+
+// Esoteric-Pull slot of population k for cell n (src/kernel.cpp:1326-1339): the pair (i,i+1), i odd,
+// is read from (n, i) and (j[i], i+1) at odd t, from (n, i+1) and (j[i], i) at even t; stores swap.
+template<typename real> static void load_f(const u64 n, real* fhn, const void* fi, const u64* j, const u64 t, const u32 q, const u64 N, const u32 st) {
+	fhn[0] = Store<real>::load(fi, n, st);
+	for(u32 i=1u; i<q; i+=2u) {
+		fhn[i   ] = Store<real>::load(fi, (u64)(t%2ull ? i    : i+1u)*N+n   , st);
+		fhn[i+1u] = Store<real>::load(fi, (u64)(t%2ull ? i+1u : i   )*N+j[i], st);
+	}
+}
+template<typename real> static void store_f(const u64 n, const real* fhn, void* fi, const u64* j, const u64 t, const u32 q, const u64 N, const u32 st) {
+	Store<real>::store(fi, n, fhn[0], st);
+	for(u32 i=1u; i<q; i+=2u) {
+		Store<real>::store(fi, (u64)(t%2ull ? i+1u : i   )*N+j[i], fhn[i   ], st);
+		Store<real>::store(fi, (u64)(t%2ull ? i    : i+1u)*N+n   , fhn[i+1u], st);
+	}
+}
+
+static inline float fmaT(const float a, const float b, const float c) { return std::fmaf(a, b, c); }
+static inline double fmaT(const double a, const double b, const double c) { return std::fma(a, b, c); }
+
+// signed sum of the non-zero terms c_d*v_d in x,y,z order; c_d in {-1,0,1} makes every product exact,
+// so this equals the reference's c(i)*vx+c(N+i)*vy+c(2N+i)*vz up to the sign of an exact zero
+template<typename real> static inline real csum(const u32 q, const u32 i, const real vx, const real vy, const real vz) {
+	const int c[3] = {cq(q, 0, i), cq(q, 1, i), cq(q, 2, i)};
+	const real v[3] = {vx, vy, vz};
+	bool first = true; real s = (real)0;
+	for(int d=0; d<3; d++) {
+		if(c[d]==0) continue;
+		const real term = c[d]>0 ? v[d] : -v[d];
+		s = first ? term : s+term;
+		first = false;
+	}
+	return s;
+}
+
+// calculate_f_eq (src/kernel.cpp:1004-1061): pairs (i,i+1) share u_k = 3*(c_i . u)
+template<typename real> static void calculate_f_eq(const real rho, real ux, real uy, real uz, real* feq, const u32 q) {
+	const Weights<real> W = weights<real>(q);
+	const real rhom1 = rho-(real)1;
+	const real c3 = (real)(-3)*((ux*ux+uy*uy)+uz*uz);
+	uz *= (real)3; ux *= (real)3; uy *= (real)3;
+	feq[0] = W.w0*fmaT(rho, (real)0.5*c3, rhom1);
+	for(u32 i=1u; i<q; i+=2u) {
+		const real wi = weight(W, i);
+		const real rhow = wi*rho, rhom1w = wi*rhom1;
+		const real uk = csum<real>(q, i, ux, uy, uz);
+		feq[i   ] = fmaT(rhow, fmaT((real)0.5, fmaT(uk, uk, c3),  uk), rhom1w);
+		feq[i+1u] = fmaT(rhow, fmaT((real)0.5, fmaT(uk, uk, c3), -uk), rhom1w);
+	}
+}
+
+// calculate_rho_u (src/kernel.cpp:1063-1088): rho sums f_i in index order and adds 1 last; each
+// velocity component alternates +f(positive member) -f(negative member) over the pairs in index order
+template<typename real> static void moments(const real* f, real& rho, real& mx, real& my, real& mz, const u32 q) {
+	rho = f[0];
+	for(u32 i=1u; i<q; i++) rho += f[i];
+	rho += (real)1;
+	real m[3];
+	for(int d=0; d<3; d++) {
+		bool first = true; real s = (real)0;
+		for(u32 i=1u; i<q; i+=2u) {
+			const int c = cq(q, d, i);
+			if(c==0) continue;
+			const real fp = c>0 ? f[i] : f[i+1u], fm = c>0 ? f[i+1u] : f[i];
+			s = first ? fp-fm : (s+fp)-fm;
+			first = false;
+		}
+		m[d] = s;
+	}
+	mx = m[0]; my = m[1]; mz = m[2];
+}
+template<typename real> static void calculate_rho_u(const real* f, real& rho, real& ux, real& uy, real& uz, const u32 q) {
+	real mx, my, mz;
+	moments(f, rho, mx, my, mz, q);
+	ux = mx/rho; uy = my/rho; uz = mz/rho;
+}
+
+template<typename real> static inline real sound_speed();
+template<> inline float sound_speed<float>() { return 0.57735027f; } // def_c (src/lbm.cpp:373)
+template<> inline double sound_speed<double>() { return 0.57735026918962576; }
+template<typename real> static inline real third();
+template<> inline float third<float>() { return 0.33333334f; }
+template<> inline double third<double>() { return 1.0/3.0; }
+template<typename real> static inline real clampT(const real x, const real a, const real b) { return std::fmin(std::fmax(x, a), b); }
+
+// calculate_forcing_terms (src/kernel.cpp:1091-1101), Guo forcing
+template<typename real> static void forcing_terms(const real ux, const real uy, const real uz, const real fx, const real fy, const real fz, real* Fin, const u32 q) {
+	const Weights<real> W = weights<real>(q);
+	const real uF = -third<real>()*fmaT(ux, fx, fmaT(uy, fy, uz*fz));
+	Fin[0] = (real)9*W.w0*uF;
+	for(u32 i=1u; i<q; i++) {
+		Fin[i] = (real)9*weight(W, i)*fmaT(csum<real>(q, i, fx, fy, fz), csum<real>(q, i, ux, uy, uz)+third<real>(), uF);
+	}
+}
+
+// ------------------------------------------------------------------ kernels
+template<typename real> static int initialize_t(const OracleConfig* c, void* fi, real* rho, real* u, u8* flags) {
+	const Grid G(c); const u32 q = c->q;
+	parallel_cells(G.N, c->threads, [&](const u64 n) {
+		u64 j[27]; G.neighbors(n, q, j);
+		if((flags[n]&T_BO)==T_S) { u[n] = (real)0; u[G.N+n] = (real)0; u[2ull*G.N+n] = (real)0; } // src/kernel.cpp:1370-1373
+		real feq[27];
+		calculate_f_eq<real>(rho[n], u[n], u[G.N+n], u[2ull*G.N+n], feq, q);
+		store_f<real>(n, feq, fi, j, 1ull, q, G.N, c->storage); // odd parity baked in (src/kernel.cpp:1429)
+	});
+	return 0;
+}
+
+// force shift + clamp shared by stream_collide and update_fields (src/kernel.cpp:1550-1563, 1852-1862)
+template<typename real> static inline void shift_clamp(real& ux, real& uy, real& uz, const real rho, const real fx, const real fy, const real fz, const bool vf) {
+	const real cs = sound_speed<real>();
+	if(vf) {
+		const real rho2 = (real)0.5/rho;
+		ux = clampT(fmaT(fx, rho2, ux), -cs, cs);
+		uy = clampT(fmaT(fy, rho2, uy), -cs, cs);
+		uz = clampT(fmaT(fz, rho2, uz), -cs, cs);
+	} else {
+		ux = clampT(ux, -cs, cs); uy = clampT(uy, -cs, cs); uz = clampT(uz, -cs, cs);
+	}
+}
+
+template<typename real> static void collide_cell(real* fhn, const real rhon, const real uxn, const real uyn, const real uzn, const real fxn, const real fyn, const real fzn,
+                                                 const bool is_e, const OracleConfig* c) {
+	const u32 q = c->q;
+	const bool vf = (c->ext&EXT_VOLUME_FORCE)!=0u;
+	real Fin[27], feq[27];
+	if(vf) forcing_terms<real>(uxn, uyn, uzn, fxn, fyn, fzn, Fin, q); else for(u32 i=0u; i<q; i++) Fin[i] = (real)0;
+	calculate_f_eq<real>(rhon, uxn, uyn, uzn, feq, q);
+	const real w = (real)c->w;
+	if(!c->trt) { // SRT (src/kernel.cpp:1595-1604)
+		if(vf) { const real c_tau = fmaT(w, (real)(-0.5), (real)1); for(u32 i=0u; i<q; i++) Fin[i] *= c_tau; }
+		for(u32 i=0u; i<q; i++) fhn[i] = is_e ? feq[i] : fmaT((real)1-w, fhn[i], fmaT(w, feq[i], Fin[i]));
+	} else { // TRT (src/kernel.cpp:1605-1633)
+		const real wp = w;
+		const real wm = (real)1/((real)0.1875/((real)1/w-(real)0.5)+(real)0.5);
+		if(vf) {
+			const real c_taup = fmaT(wp, (real)(-0.25), (real)0.5), c_taum = fmaT(wm, (real)(-0.25), (real)0.5);
+			real Fib[27]; Fib[0] = Fin[0];
+			for(u32 i=1u; i<q; i+=2u) { Fib[i] = Fin[i+1u]; Fib[i+1u] = Fin[i]; }
+			for(u32 i=0u; i<q; i++) Fin[i] = fmaT(c_taup, Fin[i]+Fib[i], c_taum*(Fin[i]-Fib[i]));
+		}
+		real fhb[27], feb[27];
+		fhb[0] = fhn[0]; feb[0] = feq[0];
+		for(u32 i=1u; i<q; i+=2u) { fhb[i] = fhn[i+1u]; fhb[i+1u] = fhn[i]; feb[i] = feq[i+1u]; feb[i+1u] = feq[i]; }
+		for(u32 i=0u; i<q; i++) {
+			fhn[i] = is_e ? feq[i] : fmaT((real)0.5*wp, ((feq[i]-fhn[i])+feb[i])-fhb[i], fmaT((real)0.5*wm, ((feq[i]-feb[i])-fhn[i])+fhb[i], fhn[i]+Fin[i]));
+		}
+	}
+}
+
+template<typename real> static int stream_collide_t(const OracleConfig* c, void* fi, const real* rho, const real* u, const u8* flags, const u64 t,
+                                                    const real fx, const real fy, const real fz, const real* F) {
+	const Grid G(c); const u32 q = c->q;
+	const bool eq = (c->ext&EXT_EQUILIBRIUM_BOUNDARIES)!=0u, ff = (c->ext&EXT_FORCE_FIELD)!=0u, vf = (c->ext&EXT_VOLUME_FORCE)!=0u;
+	parallel_cells(G.N, c->threads, [&](const u64 n) {
+		const u8 flagsn_bo = flags[n]&T_BO;
+		if(flagsn_bo==T_S||(flags[n]&T_SU)==T_G) return; // solid (implicit bounce-back through Esoteric-Pull) or gas: nothing
+		u64 j[27]; G.neighbors(n, q, j);
+		real fhn[27];
+		load_f<real>(n, fhn, fi, j, t, q, G.N, c->storage);
+		real rhon, uxn, uyn, uzn;
+		const bool is_e = eq && flagsn_bo==T_E;
+		if(is_e) { rhon = rho[n]; uxn = u[n]; uyn = u[G.N+n]; uzn = u[2ull*G.N+n]; }
+		else calculate_rho_u<real>(fhn, rhon, uxn, uyn, uzn, q);
+		real fxn = fx, fyn = fy, fzn = fz;
+		if(ff) { fxn += F[n]; fyn += F[G.N+n]; fzn += F[2ull*G.N+n]; }
+		shift_clamp<real>(uxn, uyn, uzn, rhon, fxn, fyn, fzn, vf);
+		collide_cell<real>(fhn, rhon, uxn, uyn, uzn, fxn, fyn, fzn, is_e, c);
+		store_f<real>(n, fhn, fi, j, t, q, G.N, c->storage);
+	});
+	return 0;
+}
+
+template<typename real> static int update_fields_t(const OracleConfig* c, const void* fi, real* rho, real* u, const u8* flags, const u64 t,
+                                                   const real fx, const real fy, const real fz, const real* F) {
+	const Grid G(c); const u32 q = c->q;
+	const bool eq = (c->ext&EXT_EQUILIBRIUM_BOUNDARIES)!=0u, ff = (c->ext&EXT_FORCE_FIELD)!=0u, vf = (c->ext&EXT_VOLUME_FORCE)!=0u;
+	parallel_cells(G.N, c->threads, [&](const u64 n) {
+		const u8 flagsn_bo = flags[n]&T_BO;
+		if(flagsn_bo==T_S||(flags[n]&T_SU)==T_G) return;
+		u64 j[27]; G.neighbors(n, q, j);
+		real fhn[27];
+		load_f<real>(n, fhn, fi, j, t, q, G.N, c->storage);
+		real rhon, uxn, uyn, uzn;
+		calculate_rho_u<real>(fhn, rhon, uxn, uyn, uzn, q);
+		real fxn = fx, fyn = fy, fzn = fz;
+		if(ff) { fxn += F[n]; fyn += F[G.N+n]; fzn += F[2ull*G.N+n]; }
+		shift_clamp<real>(uxn, uyn, uzn, rhon, fxn, fyn, fzn, vf);
+		if(eq && flagsn_bo==T_E) return; // preset rho/u of TYPE_E cells stay
+		rho[n] = rhon; u[n] = uxn; u[G.N+n] = uyn; u[2ull*G.N+n] = uzn;
+	});
+	return 0;
+}
+
+template<typename real> static int update_force_field_t(const OracleConfig* c, const void* fi, const u8* flags, const u64 t, real* F) {
+	const Grid G(c); const u32 q = c->q;
+	parallel_cells(G.N, c->threads, [&](const u64 n) {
+		if((flags[n]&T_BO)!=T_S) return;
+		u64 j[27]; G.neighbors(n, q, j);
+		real fhn[27];
+		load_f<real>(n, fhn, fi, j, t, q, G.N, c->storage);
+		real Fb, fx, fy, fz;
+		calculate_rho_u<real>(fhn, Fb, fx, fy, fz, q);
+		const real s = (real)2*Fb;
+		F[n] = s*fx; F[G.N+n] = s*fy; F[2ull*G.N+n] = s*fz;
+	});
+	return 0;
+}
+
+// object reductions: masked sums over flags==marker (src/kernel.cpp:1901-1959), accumulated in FP64
+static int object_sum_impl(const OracleConfig* c, const int kind, const float* F, const u8* flags, const u8 marker,
+                           const double cx, const double cy, const double cz, double* out) {
+	const Grid G(c);
+	double s[4] = {0.0, 0.0, 0.0, 0.0};
+	for(u64 n=0ull; n<G.N; n++) {
+		if(flags[n]!=marker) continue;
+		u32 x, y, z; G.coords(n, x, y, z);
+		const double px = (double)((float)x+0.5f-0.5f*(float)G.Nx), py = (double)((float)y+0.5f-0.5f*(float)G.Ny), pz = (double)((float)z+0.5f-0.5f*(float)G.Nz);
+		if(kind==0) { s[0] += px; s[1] += py; s[2] += pz; s[3] += 1.0; }
+		else {
+			const double Fx = F[n], Fy = F[G.N+n], Fz = F[2ull*G.N+n];
+			if(kind==1) { s[0] += Fx; s[1] += Fy; s[2] += Fz; }
+			else {
+				const double rx = px-cx, ry = py-cy, rz = pz-cz;
+				s[0] += ry*Fz-rz*Fy; s[1] += rz*Fx-rx*Fz; s[2] += rx*Fy-ry*Fx;
+			}
+		}
+	}
+	for(int i=0; i<4; i++) out[i] = s[i];
+	return 0;
+}
+
+// ------------------------------------------------------------------ voxelization (src/kernel.cpp:2267-2357), FP32
+struct f3 { float x, y, z; };
+static inline f3 sub(const f3 a, const f3 b) { return {a.x-b.x, a.y-b.y, a.z-b.z}; }
+static inline f3 add(const f3 a, const f3 b) { return {a.x+b.x, a.y+b.y, a.z+b.z}; }
+static inline f3 cross(const f3 a, const f3 b) { return {a.y*b.z-a.z*b.y, a.z*b.x-a.x*b.z, a.x*b.y-a.y*b.x}; }
+static inline float dot(const f3 a, const f3 b) { return a.x*b.x+a.y*b.y+a.z*b.z; }
+static inline int clampi(const int x, const int a, const int b) { return x<a ? a : x>b ? b : x; }
+
+static int voxelize_impl(const OracleConfig* c, const u32 direction, void* fi, float* u, u8* flags, const u64 t, const u8 flag,
+                         const float* p0, const float* p1, const float* p2, const float* bbu) {
+	const Grid G(c); const u32 q = c->q;
+	const u32 Nx = G.Nx, Ny = G.Ny, Nz = G.Nz;
+	const u64 A = direction==0u ? (u64)Ny*Nz : direction==1u ? (u64)Nz*Nx : (u64)Nx*Ny;
+	u32 triangle_number; std::memcpy(&triangle_number, &bbu[0], 4);
+	const float x0=bbu[1], y0=bbu[2], z0=bbu[3], x1=bbu[4], y1=bbu[5], z1=bbu[6];
+	const float cx=bbu[7], cy=bbu[8], cz=bbu[9], ux=bbu[10], uy=bbu[11], uz=bbu[12], rx=bbu[13], ry=bbu[14], rz=bbu[15];
+	const u32 hmin = direction==0u ? (u32)clampi((int)x0, 0, (int)Nx-1) : direction==1u ? (u32)clampi((int)y0, 0, (int)Ny-1) : (u32)clampi((int)z0, 0, (int)Nz-1);
+	const u32 hmax = direction==0u ? (u32)clampi((int)x1, 0, (int)Nx-1) : direction==1u ? (u32)clampi((int)y1, 0, (int)Ny-1) : (u32)clampi((int)z1, 0, (int)Nz-1);
+	const f3 offset = {0.5f*(float)(int)Nx-0.5f, 0.5f*(float)(int)Ny-0.5f, 0.5f*(float)(int)Nz-0.5f};
+	const f3 r_dir = {(float)(direction==0u), (float)(direction==1u), (float)(direction==2u)};
+	const bool set_u = ux*ux+uy*uy+uz*uz+rx*rx+ry*ry+rz*rz>0.0f;
+	parallel_cells(A, c->threads, [&](const u64 ai) {
+		const u32 a = (u32)ai;
+		u32 X, Y, Z;
+		if(direction==0u) { X = hmin; Y = a%Ny; Z = a/Ny; }
+		else if(direction==1u) { X = a/Nz; Y = hmin; Z = a%Nz; }
+		else { X = a%Nx; Y = a/Nx; Z = hmin; }
+		const f3 pos = {(float)X+0.5f-0.5f*(float)Nx, (float)Y+0.5f-0.5f*(float)Ny, (float)Z+0.5f-0.5f*(float)Nz};
+		const f3 o = add(pos, offset);
+		const bool outside = direction==0u ? o.y<y0||o.z<z0||o.y>=y1||o.z>=z1 : direction==1u ? o.x<x0||o.z<z0||o.x>=x1||o.z>=z1 : o.x<x0||o.y<y0||o.x>=x1||o.y>=y1;
+		if(outside) return;
+		u32 intersections = 0u, intersections_check = 0u;
+		u16 distances[64] = {0};
+		for(u32 i=0u; i<triangle_number; i++) {
+			const f3 a0 = {p0[3u*i], p0[3u*i+1u], p0[3u*i+2u]}, a1 = {p1[3u*i], p1[3u*i+1u], p1[3u*i+2u]}, a2 = {p2[3u*i], p2[3u*i+1u], p2[3u*i+2u]};
+			const f3 eu = sub(a1, a0), ev = sub(a2, a0), ew = sub(o, a0), h = cross(r_dir, ev), qv = cross(ew, eu);
+			const float g = dot(eu, h), f = 1.0f/g, s = f*dot(ew, h), tt = f*dot(r_dir, qv), d = f*dot(ev, qv);
+			if(g!=0.0f&&s>=0.0f&&s<1.0f&&tt>=0.0f&&s+tt<1.0f) {
+				if(d>0.0f) {
+					if(intersections<64u&&d<65536.0f) distances[intersections] = (u16)d;
+					intersections++;
+				} else {
+					intersections_check++;
+				}
+			}
+		}
+		const u32 nsort = intersections<64u ? intersections : 64u;
+		for(u32 i=1u; i<nsort; i++) { // insertion sort
+			const u16 tv = distances[i];
+			u32 k = i;
+			while(k>0u&&distances[k-1u]>tv) { distances[k] = distances[k-1u]; k--; }
+			distances[k] = tv;
+		}
+		bool inside = (intersections%2u)&&(intersections_check%2u);
+		u32 intersection = (intersections%2u)!=(intersections_check%2u);
+		const u32 h0 = direction==0u ? X : direction==1u ? Y : Z;
+		const u32 last = intersections-1u < 63u ? intersections-1u : 63u;
+		const u32 hmesh = h0+(u32)distances[last];
+		for(u32 hh=h0; hh<=hmax; hh++) {
+			while(intersection<intersections&&hh>h0+(u32)distances[intersection<63u ? intersection : 63u]) { inside = !inside; intersection++; }
+			inside = inside&&(intersection<intersections&&hh<hmesh);
+			const u32 xx = direction==0u ? hh : X, yy = direction==1u ? hh : Y, zz = direction==2u ? hh : Z;
+			const u64 n = G.index(xx, yy, zz);
+			u8 flagsn = flags[n];
+			const f3 p = add({(float)xx+0.5f-0.5f*(float)Nx, (float)yy+0.5f-0.5f*(float)Ny, (float)zz+0.5f-0.5f*(float)Nz}, offset);
+			const f3 rc = cross(sub({cx, cy, cz}, p), {rx, ry, rz});
+			const f3 u_set = {ux+rc.x, uy+rc.y, uz+rc.z};
+			if(inside) {
+				flagsn = (u8)((flagsn&~T_BO)|flag);
+				if(set_u) { u[n] = u_set.x; u[G.N+n] = u_set.y; u[2ull*G.N+n] = u_set.z; }
+			} else if((flagsn&T_BO)==T_S&&(flagsn&T_XY)==(flag&T_XY)) {
+				const f3 un = {u[n], u[G.N+n], u[2ull*G.N+n]};
+				if(un.x==u_set.x&&un.y==u_set.y&&un.z==u_set.z) {
+					if(set_u) {
+						u64 j[27]; G.neighbors(n, q, j);
+						float feq[27];
+						calculate_f_eq<float>(1.0f, un.x, un.y, un.z, feq, q);
+						store_f<float>(n, feq, fi, j, t, q, G.N, c->storage);
+					}
+					flagsn = (flagsn&T_BO)==T_MS ? (u8)(flagsn&~T_MS) : (u8)(flagsn&~flag);
+				}
+			}
+			flags[n] = flagsn;
+		}
+	});
+	return 0;
+}
+
+static int unvoxelize_impl(const OracleConfig* c, u8* flags, const u8 flag, const float x0, const float y0, const float z0, const float x1, const float y1, const float z1) {
+	const Grid G(c);
+	parallel_cells(G.N, c->threads, [&](const u64 n) {
+		u32 x, y, z; G.coords(n, x, y, z);
+		const float px = ((float)x+0.5f-0.5f*(float)G.Nx)+(0.5f*(float)(int)G.Nx-0.5f);
+		const float py = ((float)y+0.5f-0.5f*(float)G.Ny)+(0.5f*(float)(int)G.Ny-0.5f);
+		const float pz = ((float)z+0.5f-0.5f*(float)G.Nz)+(0.5f*(float)(int)G.Nz-0.5f);
+		if(px>=x0-1.0f&&py>=y0-1.0f&&pz>=z0-1.0f&&px<=x1+1.0f&&py<=y1+1.0f&&pz<=z1+1.0f) flags[n] &= (u8)~flag;
+	});
+	return 0;
+}
+
+static bool valid(const OracleConfig* c) {
+	return c && c->Nx>0u && c->Ny>0u && c->Nz>0u && (c->q==19u||c->q==27u) && c->storage<=ST_FP16C;
+}
+
+// ------------------------------------------------------------------ C ABI (ctypes)
+extern "C" {
+
+// relaxation rate as the reference bakes it into the kernel: "%f"-formatted 1/tau, tau=3*nu+0.5 in FP32
+float oracle_kernel_w(const float nu) {
+	const float tau = 3.0f*nu+0.5f;
+	char buf[64];
+	std::snprintf(buf, sizeof(buf), "%f", (double)(1.0f/tau));
+	return std::strtof(buf, nullptr);
+}
+
+int oracle_initialize_f32(const OracleConfig* c, void* fi, float* rho, float* u, u8* flags) { return valid(c) ? initialize_t<float>(c, fi, rho, u, flags) : -1; }
+int oracle_initialize_f64(const OracleConfig* c, double* fi, double* rho, double* u, u8* flags) { return valid(c) ? initialize_t<double>(c, fi, rho, u, flags) : -1; }
+
+int oracle_stream_collide_f32(const OracleConfig* c, void* fi, const float* rho, const float* u, const u8* flags, const u64 t, const float fx, const float fy, const float fz, const float* F) {
+	return valid(c) ? stream_collide_t<float>(c, fi, rho, u, flags, t, fx, fy, fz, F) : -1;
+}
+int oracle_stream_collide_f64(const OracleConfig* c, double* fi, const double* rho, const double* u, const u8* flags, const u64 t, const double fx, const double fy, const double fz, const double* F) {
+	return valid(c) ? stream_collide_t<double>(c, fi, rho, u, flags, t, fx, fy, fz, F) : -1;
+}
+// steps consecutive time steps t0, t0+1, ... (the reference's LBM::run loop, src/lbm.cpp:955-975)
+int oracle_run_f32(const OracleConfig* c, void* fi, const float* rho, const float* u, const u8* flags, const u64 t0, const u64 steps, const float fx, const float fy, const float fz, const float* F) {
+	if(!valid(c)) return -1;
+	for(u64 s=0ull; s<steps; s++) stream_collide_t<float>(c, fi, rho, u, flags, t0+s, fx, fy, fz, F);
+	return 0;
+}
+int oracle_run_f64(const OracleConfig* c, double* fi, const double* rho, const double* u, const u8* flags, const u64 t0, const u64 steps, const double fx, const double fy, const double fz, const double* F) {
+	if(!valid(c)) return -1;
+	for(u64 s=0ull; s<steps; s++) stream_collide_t<double>(c, fi, rho, u, flags, t0+s, fx, fy, fz, F);
+	return 0;
+}
+
+int oracle_update_fields_f32(const OracleConfig* c, const void* fi, float* rho, float* u, const u8* flags, const u64 t, const float fx, const float fy, const float fz, const float* F) {
+	return valid(c) ? update_fields_t<float>(c, fi, rho, u, flags, t, fx, fy, fz, F) : -1;
+}
+int oracle_update_fields_f64(const OracleConfig* c, const double* fi, double* rho, double* u, const u8* flags, const u64 t, const double fx, const double fy, const double fz, const double* F) {
+	return valid(c) ? update_fields_t<double>(c, fi, rho, u, flags, t, fx, fy, fz, F) : -1;
+}
+int oracle_update_force_field_f32(const OracleConfig* c, const void* fi, const u8* flags, const u64 t, float* F) {
+	return valid(c) ? update_force_field_t<float>(c, fi, flags, t, F) : -1;
+}
+int oracle_update_force_field_f64(const OracleConfig* c, const double* fi, const u8* flags, const u64 t, double* F) {
+	return valid(c) ? update_force_field_t<double>(c, fi, flags, t, F) : -1;
+}
+// kind 0: center of mass sums (x,y,z,count), 1: force, 2: torque about (cx,cy,cz)
+int oracle_object_sum(const OracleConfig* c, const int kind, const float* F, const u8* flags, const u8 marker, const double cx, const double cy, const double cz, double* out) {
+	return valid(c) && kind>=0 && kind<=2 ? object_sum_impl(c, kind, F, flags, marker, cx, cy, cz, out) : -1;
+}
+int oracle_voxelize_mesh(const OracleConfig* c, const u32 direction, void* fi, float* u, u8* flags, const u64 t, const u8 flag,
+                         const float* p0, const float* p1, const float* p2, const float* bbu) {
+	return valid(c) && direction<3u ? voxelize_impl(c, direction, fi, u, flags, t, flag, p0, p1, p2, bbu) : -1;
+}
+int oracle_unvoxelize_mesh(const OracleConfig* c, u8* flags, const u8 flag, const float x0, const float y0, const float z0, const float x1, const float y1, const float z1) {
+	return valid(c) ? unvoxelize_impl(c, flags, flag, x0, y0, z0, x1, y1, z1) : -1;
+}
+u16 oracle_fp16s_encode(const float x) { return float_to_half_bits_rne(x*32768.0f); }
+float oracle_fp16s_decode(const u16 h) { return half_bits_to_float(h)*3.0517578E-5f; }
+u16 oracle_fp16c_encode(const float x) { return float_to_fp16c(x); }
+float oracle_fp16c_decode(const u16 h) { return fp16c_to_float(h); }
+
+} // extern "C"
