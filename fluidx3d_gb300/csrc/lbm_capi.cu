@@ -54,6 +54,8 @@ struct lbm_domain {
 	double* partials = nullptr; // REDUCE_BLOCKS*4 doubles of reduction scratch
 	double* sum_dev = nullptr;  // 4 doubles
 	double* sum_host = nullptr; // pinned, 4 doubles
+	int* err = nullptr;         // device error word written by kernels with bounded waits
+	int path = PATH_AUTO;       // stream_collide implementation
 	uint64_t t = 0ull;
 	uint64_t t_last_update_fields = UINT64_MAX;
 	uint64_t t_last_force_field = UINT64_MAX;
@@ -63,6 +65,7 @@ struct lbm_domain {
 		StepArgs a;
 		a.g = g; a.fi = fi; a.rho = rho; a.u = u; a.flags = flags; a.F = F;
 		a.t = t; a.fx = cfg.fx; a.fy = cfg.fy; a.fz = cfg.fz; a.w = w;
+		a.err = err;
 		return a;
 	}
 	size_t field_bytes(const int field) const {
@@ -105,7 +108,26 @@ struct DeviceGuard {
 	DeviceGuard guard_((d)->device); \
 	if(guard_.err!=cudaSuccess) return cuda_fail(guard_.err, "cudaSetDevice");
 
-int launch_result(const cudaError_t e, const char* what) { return e==cudaSuccess ? LBM_OK : cuda_fail(e, what); }
+// after a synchronisation: report (and clear) an error a kernel recorded in the error word
+int check_kernel_error(lbm_domain* d) {
+	int h = 0;
+	FX3D_CUDA(cudaMemcpyAsync(&h, d->err, sizeof(int), cudaMemcpyDeviceToHost, d->stream), "cudaMemcpyAsync(error word)");
+	FX3D_CUDA(cudaStreamSynchronize(d->stream), "cudaStreamSynchronize");
+	if(h==0) return LBM_OK;
+	FX3D_CUDA(cudaMemsetAsync(d->err, 0, sizeof(int), d->stream), "cudaMemsetAsync(error word)");
+	return fail(LBM_ERR_CUDA, "a kernel gave up waiting for its bulk copies (device error code %d); the affected rows were left unchanged", h);
+}
+
+int launch_stream_collide(lbm_domain* d) {
+	const StepArgs a = d->args();
+	cudaError_t e;
+	switch(d->v.storage) {
+		case ST_FP32: e = launch_stream_collide_fp32(d->v, a, d->path, d->stream); break;
+		case ST_FP16S: e = launch_stream_collide_fp16s(d->v, a, d->path, d->stream); break;
+		default: e = launch_stream_collide_fp16c(d->v, a, d->path, d->stream); break;
+	}
+	return e==cudaSuccess ? LBM_OK : cuda_fail(e, "stream_collide");
+}
 
 int ensure_F(lbm_domain* d) {
 	if(d->F) return LBM_OK;
@@ -166,6 +188,7 @@ void release(lbm_domain* d) {
 	if(d->partials) cudaFree(d->partials);
 	if(d->sum_dev) cudaFree(d->sum_dev);
 	if(d->sum_host) cudaFreeHost(d->sum_host);
+	if(d->err) cudaFree(d->err);
 	if(d->own_stream) cudaStreamDestroy(d->own_stream);
 }
 
@@ -250,6 +273,12 @@ int lbm_domain_create(const lbm_config* c, lbm_domain** out) {
 	d->g.Nx = c->Nx; d->g.Ny = c->Ny; d->g.Nz = c->Nz; d->g.NxNy = c->Nx*c->Ny; d->g.N = N;
 	d->g.nx_inv = c->Nx==1u ? 0ull : (~0ull)/c->Nx+1ull; // ceil(2^64/Nx)
 	d->w = lbm_relaxation_rate(c->nu);
+	// stream_collide implementation: FX3D_STREAM_COLLIDE_PATH=cells|rows forces one (diagnostics and
+	// tests); the default picks the row-staged kernel wherever the lattice meets its constraints
+	if(const char* p = std::getenv("FX3D_STREAM_COLLIDE_PATH")) {
+		if(!std::strcmp(p, "cells")) d->path = PATH_CELLS;
+		else if(!std::strcmp(p, "rows")) d->path = PATH_ROWS;
+	}
 
 	cudaError_t e = cudaStreamCreateWithFlags(&d->own_stream, cudaStreamNonBlocking);
 	if(e==cudaSuccess) { d->stream = d->own_stream; e = cudaMalloc(&d->fi, d->field_bytes(LBM_FIELD_FI)); }
@@ -260,6 +289,8 @@ int lbm_domain_create(const lbm_config* c, lbm_domain** out) {
 	if(e==cudaSuccess) e = cudaMalloc(&d->partials, (size_t)REDUCE_BLOCKS*4u*sizeof(double));
 	if(e==cudaSuccess) e = cudaMalloc(&d->sum_dev, 4u*sizeof(double));
 	if(e==cudaSuccess) e = cudaMallocHost(&d->sum_host, 4u*sizeof(double));
+	if(e==cudaSuccess) e = cudaMalloc(&d->err, sizeof(int));
+	if(e==cudaSuccess) e = cudaMemsetAsync(d->err, 0, sizeof(int), d->stream);
 	if(e==cudaSuccess) e = cudaMemsetAsync(d->fi, 0, d->field_bytes(LBM_FIELD_FI), d->stream);
 	if(e==cudaSuccess) { k_fill_f32<<<1024, 256, 0, d->stream>>>(d->rho, N, 1.0f); e = cudaGetLastError(); } // rho = 1 (src/lbm.cpp:124)
 	if(e==cudaSuccess) e = cudaMemsetAsync(d->u, 0, N*12u, d->stream);
@@ -301,7 +332,7 @@ int lbm_get_stream(lbm_domain* d, void** s) {
 int lbm_synchronize(lbm_domain* d) {
 	FX3D_DOMAIN(d);
 	FX3D_CUDA(cudaStreamSynchronize(d->stream), "cudaStreamSynchronize");
-	return LBM_OK;
+	return check_kernel_error(d);
 }
 
 int lbm_write_field(lbm_domain* d, const int field, const void* host, const size_t bytes) {
@@ -325,7 +356,7 @@ int lbm_read_field(lbm_domain* d, const int field, void* host, const size_t byte
 	if(d->initialized && (field==LBM_FIELD_RHO||field==LBM_FIELD_U)) { const int r = do_update_fields(d); if(r!=LBM_OK) return r; }
 	FX3D_CUDA(cudaMemcpyAsync(host, d->field_ptr(field), bytes, cudaMemcpyDeviceToHost, d->stream), "cudaMemcpyAsync(read_field)");
 	FX3D_CUDA(cudaStreamSynchronize(d->stream), "cudaStreamSynchronize");
-	return LBM_OK;
+	return check_kernel_error(d);
 }
 
 int lbm_field_device_pointer(lbm_domain* d, const int field, void** ptr, size_t* bytes) {
@@ -359,14 +390,8 @@ int lbm_stream_collide(lbm_domain* d, const uint64_t steps) {
 	FX3D_DOMAIN(d);
 	if(!d->initialized) return fail(LBM_ERR_NOT_INITIALIZED, "lbm_stream_collide: call lbm_initialize first");
 	for(uint64_t s=0ull; s<steps; s++) {
-		const StepArgs a = d->args();
-		cudaError_t e;
-		switch(d->v.storage) {
-			case ST_FP32: e = launch_stream_collide_fp32(d->v, a, d->stream); break;
-			case ST_FP16S: e = launch_stream_collide_fp16s(d->v, a, d->stream); break;
-			default: e = launch_stream_collide_fp16c(d->v, a, d->stream); break;
-		}
-		if(e!=cudaSuccess) return cuda_fail(e, "stream_collide");
+		const int r = launch_stream_collide(d);
+		if(r!=LBM_OK) return r;
 		d->t++;
 	}
 	return LBM_OK;

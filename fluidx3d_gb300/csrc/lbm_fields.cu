@@ -15,6 +15,14 @@ namespace fx3d {
 
 constexpr int RB = 256; // threads per reduction block
 
+size_t rows_smem_bytes(const int q, const int storage, const uint32_t Nx) {
+	const size_t elem = storage==ST_FP32 ? 4u : 2u;
+	const size_t rowbytes = (size_t)Nx*elem;
+	if(rowbytes%16u!=0u) return 0u; // bulk copies move whole 16-byte units from 16-byte-aligned addresses
+	const size_t smem = (size_t)q*((rowbytes+127u)&~(size_t)127u)+16u;
+	return smem<=200u*1024u ? smem : 0u;
+}
+
 __device__ __forceinline__ double warp_sum(double v) {
 	#pragma unroll
 	for(int o=16; o>0; o>>=1) v += __shfl_down_sync(0xFFFFFFFFu, v, o);

@@ -31,14 +31,22 @@ struct StepArgs {
 	const float* F;
 	uint64_t t;
 	float fx, fy, fz, w;
+	int* err; // device error word (KERR_*), set by kernels whose bounded waits time out
 };
 
 constexpr int BLOCK = 256;
+constexpr int ROW_TPB_MAX = 256; // threads per CTA of the row-staged stream_collide
+
+// stream_collide implementation: one thread per cell with direct global loads/stores ("cells"), or
+// one CTA per x-row with the row's slots staged in shared memory by bulk copies ("rows")
+enum : int { PATH_AUTO = 0, PATH_CELLS = 1, PATH_ROWS = 2 };
+// shared-memory bytes the row-staged kernel needs, 0 if the lattice does not fit its constraints
+size_t rows_smem_bytes(int q, int storage, uint32_t Nx);
 
 // per-storage launchers (lbm_kernels_<storage>.cu)
 #define FX3D_DECLARE_LAUNCHERS(sfx) \
 	cudaError_t launch_initialize_##sfx(const Variant& v, const StepArgs& a, cudaStream_t s); \
-	cudaError_t launch_stream_collide_##sfx(const Variant& v, const StepArgs& a, cudaStream_t s); \
+	cudaError_t launch_stream_collide_##sfx(const Variant& v, const StepArgs& a, int path, cudaStream_t s); \
 	cudaError_t launch_update_fields_##sfx(const Variant& v, const StepArgs& a, cudaStream_t s); \
 	cudaError_t launch_update_force_field_##sfx(const Variant& v, const StepArgs& a, float* F, cudaStream_t s);
 FX3D_DECLARE_LAUNCHERS(fp32)

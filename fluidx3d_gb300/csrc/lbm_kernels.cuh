@@ -10,6 +10,7 @@
 #pragma once
 #include "lbm_scheme.cuh"
 #include "lbm_internal.h"
+#include "lbm_bulk.cuh"
 
 namespace fx3d {
 
@@ -88,6 +89,92 @@ template<int Q, int ST, bool TRT, int EXT> __global__ void __launch_bounds__(BLO
 	store_f<Q, ST>((T*)a.fi, g.N, n, nb, odd, f);
 }
 
+// Row-staged stream_collide. At either parity the cells of one x-row (y,z) own exactly Q whole
+// rows of the DDF array: row (y,z) of array 0 and of the arrays of their "own" slots, and for each
+// pair (i,i+1) row (y+c_iy, z+c_iz) of the array of their neighbour slots, rotated by c_ix
+// (periodic in x). One CTA per x-row bulk-loads those Q rows into shared memory (cp.async.bulk,
+// completion on one mbarrier), collides every cell of the row from shared memory and bulk-stores
+// the same Q rows back. Every global access is a whole 16-byte-aligned row, no data in flight sits
+// in registers, and slots of solid cells go back unchanged. Rows are owned by exactly one CTA per
+// parity, so CTAs never touch each other's rows.
+template<int Q, int ST> struct RowLayout {
+	typedef typename Codec<ST>::T T;
+	uint32_t rowbytes, stride; // bytes of one row, and its 128-byte-aligned pitch in shared memory
+	__host__ __device__ explicit RowLayout(const uint32_t Nx) : rowbytes(Nx*(uint32_t)sizeof(T)), stride((Nx*(uint32_t)sizeof(T)+127u)&~127u) {}
+	__host__ __device__ size_t smem_bytes() const { return (size_t)Q*stride+16u; }
+};
+
+template<int Q, int ST, bool TRT, int EXT> __global__ void __launch_bounds__(ROW_TPB_MAX) k_stream_collide_rows(const StepArgs a) {
+	typedef typename Codec<ST>::T T;
+	constexpr bool VF = (EXT&EXT_VF)!=0, EQ = (EXT&EXT_EQ)!=0;
+	extern __shared__ __align__(128) unsigned char smem[];
+	const Grid& g = grid_of(a.g);
+	const uint32_t Nx = g.Nx, Ny = g.Ny, Nz = g.Nz, y = blockIdx.x, z = blockIdx.y;
+	const RowLayout<Q, ST> L(Nx);
+	uint64_t* bar = reinterpret_cast<uint64_t*>(smem+(size_t)Q*L.stride);
+	auto srow = [&](const int s) { return reinterpret_cast<T*>(smem+(size_t)s*L.stride); };
+	const bool odd = (a.t&1ull)!=0ull;
+	const uint64_t N = g.N;
+	const uint64_t row0 = ((uint64_t)z*Ny+y)*Nx;
+	T* fi = (T*)a.fi;
+	// global start of the row held in shared-memory slot s (0; i: own slot; i+1: neighbour slot)
+	auto grow = [&](auto ic) -> uint64_t {
+		constexpr int s = decltype(ic)::value;
+		if constexpr(s==0) return row0;
+		else if constexpr(s%2==1) return (uint64_t)(odd ? s : s+1)*N+row0;
+		else {
+			constexpr int i = s-1, cy = vs_c(1, i), cz = vs_c(2, i);
+			const uint32_t yy = cy>0 ? (y+1u==Ny ? 0u : y+1u) : cy<0 ? (y==0u ? Ny-1u : y-1u) : y;
+			const uint32_t zz = cz>0 ? (z+1u==Nz ? 0u : z+1u) : cz<0 ? (z==0u ? Nz-1u : z-1u) : z;
+			return (uint64_t)(odd ? i+1 : i)*N+((uint64_t)zz*Ny+yy)*Nx;
+		}
+	};
+	if(threadIdx.x==0u) {
+		mbar_init(bar, 1u);
+		fence_mbar_init();
+		mbar_arrive_expect_tx(bar, (uint32_t)Q*L.rowbytes);
+		Unroll<0, Q, 1>::run([&](auto ic) { bulk_load(srow(decltype(ic)::value), fi+grow(ic), L.rowbytes, bar); });
+	}
+	__syncthreads();
+	if(!mbar_wait_bounded(bar, 0u, a.err)) {
+		mbar_wait_bounded(bar, 0u, nullptr); // give copies still in flight a second bounded chance, then leave the row untouched
+		return;
+	}
+	for(uint32_t x=threadIdx.x; x<Nx; x+=blockDim.x) {
+		const uint64_t n = row0+x;
+		const uint8_t flagsn = a.flags[n];
+		const uint8_t flagsn_bo = flagsn&TYPE_BO;
+		if(flagsn_bo==TYPE_S||(flagsn&TYPE_SU)==TYPE_G) continue;
+		const uint32_t xp = x+1u==Nx ? 0u : x+1u, xm = x==0u ? Nx-1u : x-1u;
+		float f[Q];
+		f[0] = Codec<ST>::decode(srow(0)[x]);
+		Unroll<1, Q, 2>::run([&](auto ic) {
+			constexpr int i = decltype(ic)::value, cx = vs_c(0, i);
+			const uint32_t xi = cx>0 ? xp : cx<0 ? xm : x;
+			f[i] = Codec<ST>::decode(srow(i)[x]);
+			f[i+1] = Codec<ST>::decode(srow(i+1)[xi]);
+		});
+		const bool is_e = EQ && flagsn_bo==TYPE_E;
+		float rho, ux, uy, uz, fx, fy, fz;
+		cell_rho_u<Q, EXT>(a, n, f, is_e, rho, ux, uy, uz, fx, fy, fz);
+		collide<Q, TRT, VF>(f, rho, ux, uy, uz, fx, fy, fz, is_e, a.w);
+		srow(0)[x] = Codec<ST>::encode(f[0]);
+		Unroll<1, Q, 2>::run([&](auto ic) {
+			constexpr int i = decltype(ic)::value, cx = vs_c(0, i);
+			const uint32_t xi = cx>0 ? xp : cx<0 ? xm : x;
+			srow(i+1)[xi] = Codec<ST>::encode(f[i]);
+			srow(i)[x] = Codec<ST>::encode(f[i+1]);
+		});
+	}
+	fence_proxy_async_smem();
+	__syncthreads();
+	if(threadIdx.x==0u) {
+		Unroll<0, Q, 1>::run([&](auto ic) { bulk_store(fi+grow(ic), srow(decltype(ic)::value), L.rowbytes); });
+		bulk_commit();
+		bulk_wait_read_all(); // shared memory must outlive the reads of the stores
+	}
+}
+
 template<int Q, int ST, int EXT> __global__ void __launch_bounds__(BLOCK) k_update_fields(const StepArgs a) {
 	typedef typename Codec<ST>::T T;
 	constexpr bool EQ = (EXT&EXT_EQ)!=0;
@@ -127,25 +214,39 @@ template<int Q, int ST> __global__ void __launch_bounds__(BLOCK) k_update_force_
 // ---------------------------------------------------------------- dispatch
 inline dim3 cell_grid(const GridDesc& g) { return dim3((g.NxNy+BLOCK-1u)/BLOCK, g.Nz, 1u); }
 
-template<int ST, int Q, bool TRT, int EXT> inline void sc_launch(const StepArgs& a, cudaStream_t s) {
-	k_stream_collide<Q, ST, TRT, EXT><<<cell_grid(a.g), BLOCK, 0, s>>>(a);
+template<int ST, int Q, bool TRT, int EXT> inline cudaError_t sc_launch(const StepArgs& a, const bool rows, cudaStream_t s) {
+	if(rows) {
+		const RowLayout<Q, ST> L(a.g.Nx);
+		const size_t smem = L.smem_bytes();
+		if(smem>48u*1024u) { // opt in to more than 48 KB of dynamic shared memory (per device, so on every such launch)
+			const cudaError_t e = cudaFuncSetAttribute(k_stream_collide_rows<Q, ST, TRT, EXT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+			if(e!=cudaSuccess) return e;
+		}
+		const uint32_t tpb = a.g.Nx>=(uint32_t)ROW_TPB_MAX ? (uint32_t)ROW_TPB_MAX : (a.g.Nx+31u)&~31u;
+		k_stream_collide_rows<Q, ST, TRT, EXT><<<dim3(a.g.Ny, a.g.Nz, 1u), tpb, smem, s>>>(a);
+	} else {
+		k_stream_collide<Q, ST, TRT, EXT><<<cell_grid(a.g), BLOCK, 0, s>>>(a);
+	}
+	return cudaGetLastError();
 }
-template<int ST, int Q, bool TRT> inline bool sc_ext(const int ext, const StepArgs& a, cudaStream_t s) {
+template<int ST, int Q, bool TRT> inline cudaError_t sc_ext(const int ext, const StepArgs& a, const bool rows, cudaStream_t s) {
 	switch(ext) {
-		case 0:                        sc_launch<ST, Q, TRT, 0>(a, s); return true;
-		case EXT_VF:                   sc_launch<ST, Q, TRT, EXT_VF>(a, s); return true;
-		case EXT_VF|EXT_FF:            sc_launch<ST, Q, TRT, EXT_VF|EXT_FF>(a, s); return true;
-		case EXT_EQ:                   sc_launch<ST, Q, TRT, EXT_EQ>(a, s); return true;
-		case EXT_EQ|EXT_VF:            sc_launch<ST, Q, TRT, EXT_EQ|EXT_VF>(a, s); return true;
-		case EXT_EQ|EXT_VF|EXT_FF:     sc_launch<ST, Q, TRT, EXT_EQ|EXT_VF|EXT_FF>(a, s); return true;
-		default: return false;
+		case 0:                        return sc_launch<ST, Q, TRT, 0>(a, rows, s);
+		case EXT_VF:                   return sc_launch<ST, Q, TRT, EXT_VF>(a, rows, s);
+		case EXT_VF|EXT_FF:            return sc_launch<ST, Q, TRT, EXT_VF|EXT_FF>(a, rows, s);
+		case EXT_EQ:                   return sc_launch<ST, Q, TRT, EXT_EQ>(a, rows, s);
+		case EXT_EQ|EXT_VF:            return sc_launch<ST, Q, TRT, EXT_EQ|EXT_VF>(a, rows, s);
+		case EXT_EQ|EXT_VF|EXT_FF:     return sc_launch<ST, Q, TRT, EXT_EQ|EXT_VF|EXT_FF>(a, rows, s);
+		default: return cudaErrorInvalidValue;
 	}
 }
-template<int ST> cudaError_t launch_stream_collide_t(const Variant& v, const StepArgs& a, cudaStream_t s) {
-	bool ok;
-	if(v.q==19) ok = v.trt ? sc_ext<ST, 19, true>(v.ext, a, s) : sc_ext<ST, 19, false>(v.ext, a, s);
-	else ok = v.trt ? sc_ext<ST, 27, true>(v.ext, a, s) : sc_ext<ST, 27, false>(v.ext, a, s);
-	return ok ? cudaGetLastError() : cudaErrorInvalidValue;
+template<int ST> cudaError_t launch_stream_collide_t(const Variant& v, const StepArgs& a, const int path, cudaStream_t s) {
+	const bool rows_ok = rows_smem_bytes(v.q, ST, a.g.Nx)!=0u;
+	if(path==PATH_ROWS && !rows_ok) return cudaErrorInvalidConfiguration;
+	const bool rows = path==PATH_ROWS || (path==PATH_AUTO && rows_ok);
+	if(v.q==19) return v.trt ? sc_ext<ST, 19, true>(v.ext, a, rows, s) : sc_ext<ST, 19, false>(v.ext, a, rows, s);
+	if(v.q==27) return v.trt ? sc_ext<ST, 27, true>(v.ext, a, rows, s) : sc_ext<ST, 27, false>(v.ext, a, rows, s);
+	return cudaErrorInvalidValue;
 }
 
 template<int ST, int Q, int EXT> inline void uf_launch(const StepArgs& a, cudaStream_t s) {
@@ -185,7 +286,7 @@ template<int ST> cudaError_t launch_update_force_field_t(const Variant& v, const
 #define FX3D_DEFINE_LAUNCHERS(sfx, ST) \
 	namespace fx3d { \
 	cudaError_t launch_initialize_##sfx(const Variant& v, const StepArgs& a, cudaStream_t s) { return launch_initialize_t<ST>(v, a, s); } \
-	cudaError_t launch_stream_collide_##sfx(const Variant& v, const StepArgs& a, cudaStream_t s) { return launch_stream_collide_t<ST>(v, a, s); } \
+	cudaError_t launch_stream_collide_##sfx(const Variant& v, const StepArgs& a, const int path, cudaStream_t s) { return launch_stream_collide_t<ST>(v, a, path, s); } \
 	cudaError_t launch_update_fields_##sfx(const Variant& v, const StepArgs& a, cudaStream_t s) { return launch_update_fields_t<ST>(v, a, s); } \
 	cudaError_t launch_update_force_field_##sfx(const Variant& v, const StepArgs& a, float* F, cudaStream_t s) { return launch_update_force_field_t<ST>(v, a, F, s); } \
 	}

@@ -53,6 +53,8 @@ template<int I> __device__ __forceinline__ float csum(const float vx, const floa
 template<int ST> struct Codec;
 template<> struct Codec<ST_FP32> {
 	typedef float T;
+	static __device__ __forceinline__ float decode(const float x) { return x; }
+	static __device__ __forceinline__ float encode(const float x) { return x; }
 	static __device__ __forceinline__ float load(const T* p) { return *p; }
 	static __device__ __forceinline__ void store(T* p, const float x) { *p = x; }
 };

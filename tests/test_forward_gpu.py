@@ -32,8 +32,15 @@ def make_oracle(case):
     return o
 
 
+@pytest.fixture(params=["rows", "cells"])
+def path(request, monkeypatch):
+    """Both stream_collide implementations: row-staged bulk copies, and one thread per cell."""
+    monkeypatch.setenv("FX3D_STREAM_COLLIDE_PATH", request.param)
+    return request.param
+
+
 @pytest.mark.parametrize("case", LC.CASES, ids=[c.name for c in LC.CASES])
-def test_gpu_matches_reference_fixture(case, gpu, golden_dir):
+def test_gpu_matches_reference_fixture(case, gpu, golden_dir, path):
     g = np.load(os.path.join(golden_dir, f"lbm_{case.name}.npz"))
     with make_gpu(case) as lbm:
         lbm.run(case.steps)
@@ -49,15 +56,17 @@ def test_gpu_matches_reference_fixture(case, gpu, golden_dir):
 
 
 @pytest.mark.parametrize("case", LC.CASES, ids=[c.name for c in LC.CASES])
-def test_gpu_matches_oracle_step_by_step(case, gpu):
+def test_gpu_matches_oracle_step_by_step(case, gpu, path):
     """DDFs after initialize and after 1, 2, 5 steps (both parities); fields at each stop."""
     o = make_oracle(case)
     with make_gpu(case) as lbm:
         o.initialize()
         lbm.initialize()
         assert np.array_equal(lbm.read_ddfs(), o.fi)
+        # reading u after initialize runs update_fields first, as the reference's lazy read does
+        o.update_fields(*case.force)
         lbm.u.read_from_device()
-        assert np.array_equal(lbm.u.data, o.u)  # initialize zeroes u in solid cells
+        assert np.array_equal(lbm.u.data, o.u)
         for steps in (1, 1, 3):
             o.run(steps, *case.force)
             lbm.run(steps)
@@ -69,7 +78,7 @@ def test_gpu_matches_oracle_step_by_step(case, gpu):
             assert np.array_equal(lbm.rho.data, o.rho) and np.array_equal(lbm.u.data, o.u)
 
 
-def test_taylor_green_64_bit_identical_to_reference(gpu, golden_dir):
+def test_taylor_green_64_bit_identical_to_reference(gpu, golden_dir, path):
     """64^3 TGV, D3Q19 SRT FP32, tau=0.6, 1000 steps: rho/u/DDF bytes equal the reference's."""
     g = np.load(os.path.join(golden_dir, "tgv64.npz"))
     case = LC.TGV64
@@ -114,4 +123,26 @@ def test_set_force_between_steps(gpu):
         lbm.set_f(0.0, 2e-5, -1e-5)
         lbm.run(4)
         o.run(4, 0.0, 2e-5, -1e-5)
+        assert np.array_equal(lbm.read_ddfs(), o.fi)
+
+
+@pytest.mark.parametrize("storage", ["fp32", "fp16s", "fp16c"])
+@pytest.mark.parametrize("shape", [(13, 9, 7), (24, 5, 3), (40, 1, 2)])
+def test_odd_lattices_random_flags(storage, shape, gpu):
+    """Lattices whose rows are not 16-byte multiples (row-staging falls back to one thread per cell),
+    flat ones, random solid/equilibrium cells and random fields: bit-identical to the oracle."""
+    Nx, Ny, Nz = shape
+    N = Nx * Ny * Nz
+    rng = np.random.default_rng(Nx * 1000 + Ny * 10 + Nz)
+    flags = rng.choice(np.array([0, 0, 0, 0, 0x01, 0x02, 0x41], np.uint8), N)
+    f = dict(rho=(1.0 + rng.normal(0, 0.01, N)).astype(np.float32), u=rng.normal(0, 0.03, 3 * N).astype(np.float32),
+             flags=flags, F=rng.normal(0, 2e-4, 3 * N).astype(np.float32))
+    ext = ("eq", "ff", "vf")
+    o = oracle.Oracle(Nx, Ny, Nz, q=19, collision="trt", storage=storage, extensions=ext, nu=0.02)
+    o.rho[:], o.u[:], o.flags[:], o.F[:] = f["rho"], f["u"], f["flags"], f["F"]
+    with LBM(Nx, Ny, Nz, 0.02, 3e-5, -1e-5, 2e-5, collision="trt", storage=storage, extensions=ext) as lbm:
+        lbm.rho.data[:], lbm.u.data[:], lbm.flags.data[:], lbm.F.data[:] = f["rho"], f["u"], f["flags"], f["F"]
+        o.initialize()
+        lbm.run(5)
+        o.run(5, 3e-5, -1e-5, 2e-5)
         assert np.array_equal(lbm.read_ddfs(), o.fi)
