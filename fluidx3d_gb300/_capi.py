@@ -16,6 +16,8 @@ SRT, TRT = 0, 1
 FP32, FP16S, FP16C = 0, 1, 2
 EXT_VOLUME_FORCE, EXT_FORCE_FIELD, EXT_EQUILIBRIUM_BOUNDARIES = 1, 2, 4
 FIELD_RHO, FIELD_U, FIELD_FLAGS, FIELD_F, FIELD_FI = 0, 1, 2, 3, 4
+ARITH_AUTO, ARITH_EXACT, ARITH_FAST = 0, 1, 2
+ARITHMETICS = {"auto": ARITH_AUTO, "exact": ARITH_EXACT, "fast": ARITH_FAST}
 
 COLLISIONS = {"srt": SRT, "trt": TRT}
 STORAGES = {"fp32": FP32, "fp16s": FP16S, "fp16c": FP16C}
@@ -33,8 +35,22 @@ class LBMConfig(ctypes.Structure):
     _fields_ = [("Nx", ctypes.c_uint32), ("Ny", ctypes.c_uint32), ("Nz", ctypes.c_uint32),
                 ("velocity_set", ctypes.c_uint32), ("collision", ctypes.c_uint32), ("storage", ctypes.c_uint32),
                 ("extensions", ctypes.c_uint32), ("device", ctypes.c_int32),
-                ("nu", ctypes.c_float), ("fx", ctypes.c_float), ("fy", ctypes.c_float), ("fz", ctypes.c_float)]
+                ("nu", ctypes.c_float), ("fx", ctypes.c_float), ("fy", ctypes.c_float), ("fz", ctypes.c_float),
+                ("arithmetic", ctypes.c_uint32)]
 
+
+class AdjointConfig(ctypes.Structure):
+    _fields_ = [("steps", ctypes.c_uint64), ("checkpoint_interval", ctypes.c_uint64), ("objective", ctypes.c_uint32),
+                ("plane_x", ctypes.c_uint32), ("marker", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
+                ("window_begin", ctypes.c_uint64), ("window_end", ctypes.c_uint64)]
+
+
+class AdjointStats(ctypes.Structure):
+    _fields_ = [("forward_ms", ctypes.c_double), ("recompute_ms", ctypes.c_double), ("adjoint_ms", ctypes.c_double),
+                ("workspace_bytes", ctypes.c_uint64), ("levels", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+
+OBJECTIVES = {"ke_plane": 1, "drag_x": 2}
 
 # every symbol include/lbm_capi.h declares, with (argtypes, restype)
 _v, _i, _u8, _u32, _u64, _f, _d, _sz = (ctypes.c_void_p, ctypes.c_int, ctypes.c_uint8, ctypes.c_uint32, ctypes.c_uint64,
@@ -66,6 +82,7 @@ SIGNATURES = {
     "lbm_object_torque": ([_v, _u8, _d, _d, _d, ctypes.POINTER(_d)], _i),
     "lbm_voxelize_mesh": ([_v, _v, _v, _v, _u32, _u8, ctypes.POINTER(_f), ctypes.POINTER(_f), ctypes.POINTER(_f)], _i),
     "lbm_unvoxelize_mesh": ([_v, ctypes.POINTER(_f), ctypes.POINTER(_f), _u8], _i),
+    "lbm_run_adjoint": ([_v, ctypes.POINTER(AdjointConfig), ctypes.POINTER(_d), _v, ctypes.POINTER(AdjointStats)], _i),
     "lbm_host_alloc": ([_sz, ctypes.POINTER(_v)], _i),
     "lbm_host_free": ([_v], _i),
     "lbm_last_error": ([], ctypes.c_char_p),

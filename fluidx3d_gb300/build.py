@@ -1,9 +1,9 @@
 """Builds the sm_103a shared library of the solver core in-tree.
 
 One nvcc process per translation unit (they compile in parallel), then one link step into
-fluidx3d_gb300/_lib/libfluidx3d_gb300.so. Everything is compiled for sm_103a only, with FP32
-arithmetic kept uncontracted (-fmad=false) and IEEE division/square root, so every kernel gives the
-scheme's exact FP32 result.
+fluidx3d_gb300/_lib/libfluidx3d_gb300.so. Everything is compiled for sm_103a only. The exact
+arithmetic mode spells every rounding as an intrinsic, so it stays uncontracted while the fast mode
+lets nvcc contract multiply-adds; host code is compiled without contraction (-ffp-contract=off).
 """
 from __future__ import annotations
 
@@ -22,7 +22,7 @@ LIB_NAME = "libfluidx3d_gb300.so"
 LIB_PATH = os.path.join(OUT_DIR, LIB_NAME)
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false",
+NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-prec-div=true", "-prec-sqrt=true", "-ftz=false",
               "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC,-ffp-contract=off,-O2", "-I", INCLUDE, "-I", CSRC]
 
 

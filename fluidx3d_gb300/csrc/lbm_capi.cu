@@ -1,6 +1,7 @@
 // C-ABI implementation (include/lbm_capi.h): owns the device buffers of one LBM domain, keeps the
 // time step and the lazy-update bookkeeping of the reference's LBM_Domain (src/lbm.cpp:96-332), and
 // launches the sm_103a kernels. No entry point exits the process or throws across the ABI.
+#include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
@@ -9,6 +10,7 @@
 #include <new>
 #include "lbm_capi.h"
 #include "lbm_internal.h"
+#include "lbm_adjoint.h"
 
 using namespace fx3d;
 
@@ -44,6 +46,7 @@ struct lbm_domain {
 	Variant v;
 	GridDesc g;
 	float w;
+	Rates rates;
 	int device;
 	cudaStream_t own_stream = nullptr, stream = nullptr;
 	void* fi = nullptr;
@@ -63,9 +66,10 @@ struct lbm_domain {
 
 	StepArgs args() const {
 		StepArgs a;
-		a.g = g; a.fi = fi; a.rho = rho; a.u = u; a.flags = flags; a.F = F;
+		a.g = g; a.fi = fi; a.fi_dst = fi; a.rho = rho; a.u = u; a.flags = flags; a.F = F;
 		a.t = t; a.fx = cfg.fx; a.fy = cfg.fy; a.fz = cfg.fz; a.w = w;
 		a.err = err;
+		a.omw = rates.omw; a.c_tau = rates.c_tau; a.hp = rates.hp; a.hm = rates.hm; a.c_taup = rates.c_taup; a.c_taum = rates.c_taum;
 		return a;
 	}
 	size_t field_bytes(const int field) const {
@@ -194,6 +198,23 @@ void release(lbm_domain* d) {
 
 } // namespace
 
+namespace fx3d {
+// the reference computes these per cell in the kernel (src/kernel.cpp:1598, 1606-1609); the same FP32
+// operations on the host (compiled without contraction) give the same values once per domain
+Rates make_rates(const float w) {
+	Rates r;
+	r.w = w;
+	r.omw = 1.0f-w;
+	r.c_tau = std::fmaf(w, -0.5f, 1.0f);
+	const float wm = 1.0f/(0.1875f/(1.0f/w-0.5f)+0.5f);
+	r.hp = 0.5f*w;
+	r.hm = 0.5f*wm;
+	r.c_taup = std::fmaf(w, -0.25f, 0.5f);
+	r.c_taum = std::fmaf(wm, -0.25f, 0.5f);
+	return r;
+}
+} // namespace fx3d
+
 extern "C" {
 
 const char* lbm_last_error(void) { return g_last_error.c_str(); }
@@ -241,6 +262,7 @@ int lbm_domain_create(const lbm_config* c, lbm_domain** out) {
 	if(c->collision>LBM_TRT) return fail(LBM_ERR_INVALID_ARGUMENT, "collision must be LBM_SRT or LBM_TRT");
 	if(c->storage>LBM_FP16C) return fail(LBM_ERR_INVALID_ARGUMENT, "storage must be LBM_FP32, LBM_FP16S or LBM_FP16C");
 	if(c->extensions&~7u) return fail(LBM_ERR_INVALID_ARGUMENT, "unknown extension bits 0x%x", c->extensions&~7u);
+	if(c->arithmetic>LBM_ARITH_FAST) return fail(LBM_ERR_INVALID_ARGUMENT, "arithmetic must be LBM_ARITH_AUTO, LBM_ARITH_EXACT or LBM_ARITH_FAST");
 	if(!(c->nu>0.0f)) return fail(LBM_ERR_INVALID_ARGUMENT, c->nu==0.0f ? "Viscosity cannot be 0." : "Viscosity cannot be negative.");
 	if(!(c->extensions&LBM_EXT_VOLUME_FORCE)&&(c->fx!=0.0f||c->fy!=0.0f||c->fz!=0.0f))
 		return fail(LBM_ERR_INVALID_ARGUMENT, "Volume force is set, but LBM_EXT_VOLUME_FORCE is not enabled.");
@@ -270,9 +292,11 @@ int lbm_domain_create(const lbm_config* c, lbm_domain** out) {
 	if((c->extensions&LBM_EXT_FORCE_FIELD)&&(c->extensions&LBM_EXT_VOLUME_FORCE)) ext |= EXT_FF; // F acts on the fluid only with VOLUME_FORCE
 	if(c->extensions&LBM_EXT_EQUILIBRIUM_BOUNDARIES) ext |= EXT_EQ;
 	d->v.ext = ext;
+	d->v.fast = c->arithmetic==LBM_ARITH_FAST || (c->arithmetic==LBM_ARITH_AUTO && c->storage!=LBM_FP32);
 	d->g.Nx = c->Nx; d->g.Ny = c->Ny; d->g.Nz = c->Nz; d->g.NxNy = c->Nx*c->Ny; d->g.N = N;
 	d->g.nx_inv = c->Nx==1u ? 0ull : (~0ull)/c->Nx+1ull; // ceil(2^64/Nx)
 	d->w = lbm_relaxation_rate(c->nu);
+	d->rates = make_rates(d->w);
 	// stream_collide implementation: FX3D_STREAM_COLLIDE_PATH=cells|rows forces one (diagnostics and
 	// tests); the default picks the row-staged kernel wherever the lattice meets its constraints
 	if(const char* p = std::getenv("FX3D_STREAM_COLLIDE_PATH")) {
@@ -522,3 +546,163 @@ int lbm_unvoxelize_mesh(lbm_domain* d, const float pmin[3], const float pmax[3],
 }
 
 } // extern "C"
+
+// ==================================================================== adjoint driver
+namespace {
+
+struct DeviceBuffer { // freed on scope exit
+	void* p = nullptr;
+	~DeviceBuffer() { if(p) cudaFree(p); }
+};
+
+// f^{k+1} = step(f^k) from src into dst (row-staged kernel out of place; otherwise copy, then in place)
+int step_out_of_place(lbm_domain* d, const void* src, void* dst, const uint64_t t) {
+	StepArgs a = d->args();
+	a.t = t;
+	const bool rows = d->path!=PATH_CELLS && row_plan(d->v.q, d->v.storage, d->g.Nx, d->g.Ny, d->g.Nz).stages!=0u;
+	if(rows) { a.fi = const_cast<void*>(src); a.fi_dst = dst; }
+	else {
+		FX3D_CUDA(cudaMemcpyAsync(dst, src, d->field_bytes(LBM_FIELD_FI), cudaMemcpyDeviceToDevice, d->stream), "cudaMemcpyAsync(state)");
+		a.fi = dst; a.fi_dst = dst;
+	}
+	cudaError_t e;
+	const int path = rows ? PATH_ROWS : PATH_CELLS;
+	switch(d->v.storage) {
+		case ST_FP32: e = launch_stream_collide_fp32(d->v, a, path, d->stream); break;
+		case ST_FP16S: e = launch_stream_collide_fp16s(d->v, a, path, d->stream); break;
+		default: e = launch_stream_collide_fp16c(d->v, a, path, d->stream); break;
+	}
+	return e==cudaSuccess ? LBM_OK : cuda_fail(e, "stream_collide (recompute)");
+}
+
+struct EventTimer {
+	cudaEvent_t a = nullptr, b = nullptr;
+	explicit EventTimer(cudaStream_t s) { cudaEventCreate(&a); cudaEventCreate(&b); cudaEventRecord(a, s); }
+	double stop(cudaStream_t s) { float ms = 0.0f; cudaEventRecord(b, s); cudaEventSynchronize(b); cudaEventElapsedTime(&ms, a, b); return ms; }
+	~EventTimer() { if(a) cudaEventDestroy(a); if(b) cudaEventDestroy(b); }
+};
+
+} // namespace
+
+extern "C" int lbm_run_adjoint(lbm_domain* d, const lbm_adjoint_config* cfg, double* objective, float* gradient, lbm_adjoint_stats* stats) {
+	FX3D_DOMAIN(d);
+	if(!cfg) return fail(LBM_ERR_INVALID_ARGUMENT, "lbm_run_adjoint: NULL config");
+	if(!d->initialized) return fail(LBM_ERR_NOT_INITIALIZED, "lbm_run_adjoint: call lbm_initialize first");
+	if(!adjoint_supported(d->v) || !d->F) return fail(LBM_ERR_UNSUPPORTED, "lbm_run_adjoint needs LBM_EXT_VOLUME_FORCE and LBM_EXT_FORCE_FIELD (F is the design variable)");
+	if(cfg->steps==0ull||cfg->checkpoint_interval==0ull) return fail(LBM_ERR_INVALID_ARGUMENT, "lbm_run_adjoint: steps and checkpoint_interval must be >= 1");
+	if(cfg->objective!=LBM_OBJECTIVE_KINETIC_ENERGY_PLANE_X && cfg->objective!=LBM_OBJECTIVE_DRAG_X) return fail(LBM_ERR_INVALID_ARGUMENT, "lbm_run_adjoint: unknown objective %u", cfg->objective);
+	if(cfg->objective==LBM_OBJECTIVE_KINETIC_ENERGY_PLANE_X && cfg->plane_x>=d->g.Nx) return fail(LBM_ERR_INVALID_ARGUMENT, "lbm_run_adjoint: plane_x outside the lattice");
+	if(cfg->window_end<cfg->window_begin) return fail(LBM_ERR_INVALID_ARGUMENT, "lbm_run_adjoint: empty objective window");
+	const uint64_t t0 = d->t, T = cfg->steps, K = cfg->checkpoint_interval, N = d->g.N;
+	const size_t SB = d->field_bytes(LBM_FIELD_FI);
+	const uint64_t nsnap = (T+K-1ull)/K;
+	// objective weight: 1/(window length) (x 1/(fluid cells of the plane) for the kinetic energy)
+	double weight = 1.0/(double)(cfg->window_end-cfg->window_begin+1ull);
+	if(cfg->objective==LBM_OBJECTIVE_KINETIC_ENERGY_PLANE_X) {
+		std::string flags(N, '\0');
+		FX3D_CUDA(cudaMemcpyAsync(&flags[0], d->flags, N, cudaMemcpyDeviceToHost, d->stream), "cudaMemcpyAsync(flags)");
+		FX3D_CUDA(cudaStreamSynchronize(d->stream), "cudaStreamSynchronize");
+		uint64_t cells = 0ull;
+		const bool eq = (d->v.ext&EXT_EQ)!=0;
+		for(uint64_t n=cfg->plane_x; n<N; n+=d->g.Nx) {
+			const uint8_t fl = (uint8_t)flags[n];
+			if((fl&3u)!=1u && (fl&0x38u)!=0x20u && !(eq && (fl&3u)==2u)) cells++;
+		}
+		if(cells==0ull) return fail(LBM_ERR_INVALID_ARGUMENT, "lbm_run_adjoint: plane x=%u has no fluid cells", cfg->plane_x);
+		weight /= (double)cells;
+	}
+	// workspace: snapshots, segment states (all of a segment, or sub-snapshots + a sub-segment), lambda, gradient, J
+	size_t free_b = 0u, total_b = 0u;
+	FX3D_CUDA(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo");
+	const size_t fixed = (size_t)d->cfg.velocity_set*N*4u+N*12u+64u;
+	const size_t margin = 512ull<<20;
+	uint64_t K2 = K; // states kept per (sub-)segment
+	uint32_t levels = 1u;
+	size_t need = (nsnap+K)*SB+fixed;
+	if(need+margin>free_b) {
+		levels = 2u;
+		K2 = 2ull; while(K2*K2<K) K2++; // >= 2: the recomputation ping-pongs between two states
+		need = (nsnap+(K+K2-1ull)/K2+K2)*SB+fixed;
+		if(need+margin>free_b) return fail(LBM_ERR_OUT_OF_MEMORY, "lbm_run_adjoint: %zu MB of workspace needed, %zu MB free; increase checkpoint_interval", need>>20, free_b>>20);
+	}
+	const uint64_t nsub = levels==2u ? (K+K2-1ull)/K2 : 0ull;
+	DeviceBuffer snaps, seg, sub, lam, grad, Jd;
+	FX3D_CUDA(cudaMalloc(&snaps.p, (size_t)nsnap*SB), "cudaMalloc(snapshots)");
+	FX3D_CUDA(cudaMalloc(&seg.p, (size_t)K2*SB), "cudaMalloc(segment states)");
+	if(levels==2u) FX3D_CUDA(cudaMalloc(&sub.p, (size_t)nsub*SB), "cudaMalloc(sub-snapshots)");
+	FX3D_CUDA(cudaMalloc(&lam.p, (size_t)d->cfg.velocity_set*N*4u), "cudaMalloc(adjoint DDFs)");
+	FX3D_CUDA(cudaMalloc(&grad.p, N*12u), "cudaMalloc(gradient)");
+	FX3D_CUDA(cudaMalloc(&Jd.p, sizeof(double)), "cudaMalloc(J)");
+	auto snap = [&](const uint64_t i) { return (void*)((char*)snaps.p+(size_t)i*SB); };
+	auto segs = [&](const uint64_t i) { return (void*)((char*)seg.p+(size_t)i*SB); };
+	auto subs = [&](const uint64_t i) { return (void*)((char*)sub.p+(size_t)i*SB); };
+	AdjArgs j;
+	j.lambda = (float*)lam.p; j.grad = (float*)grad.p; j.obj_kind = (int)cfg->objective; j.plane_x = cfg->plane_x; j.marker = cfg->marker;
+	auto in_window = [&](const uint64_t t) { return t>=cfg->window_begin && t<=cfg->window_end; };
+	auto args_at = [&](const uint64_t t, const void* state) { StepArgs a = d->args(); a.t = t; a.fi = const_cast<void*>(state); return a; };
+
+	// ---- forward sweep (in place on the domain's DDFs), snapshots, objective
+	FX3D_CUDA(cudaMemsetAsync(Jd.p, 0, sizeof(double), d->stream), "cudaMemsetAsync(J)");
+	EventTimer tf(d->stream);
+	for(uint64_t k=0ull; k<=T; k++) {
+		if(k%K==0ull && k<T) FX3D_CUDA(cudaMemcpyAsync(snap(k/K), d->fi, SB, cudaMemcpyDeviceToDevice, d->stream), "cudaMemcpyAsync(snapshot)");
+		if(in_window(t0+k)) {
+			j.state = d->fi; j.obj_weight = (float)weight;
+			FX3D_CUDA(launch_objective_value(d->v, args_at(t0+k, d->fi), j, d->partials, (double*)Jd.p, d->stream), "objective");
+		}
+		if(k<T) { const int r = launch_stream_collide(d); if(r!=LBM_OK) return r; d->t++; }
+	}
+	const double forward_ms = tf.stop(d->stream);
+	// ---- reverse sweep
+	double recompute_ms = 0.0, adjoint_ms = 0.0;
+	FX3D_CUDA(cudaMemsetAsync(lam.p, 0, (size_t)d->cfg.velocity_set*N*4u, d->stream), "cudaMemsetAsync(lambda)");
+	FX3D_CUDA(cudaMemsetAsync(grad.p, 0, N*12u, d->stream), "cudaMemsetAsync(gradient)");
+	if(in_window(t0+T)) {
+		j.state = d->fi; j.obj_weight = (float)weight;
+		FX3D_CUDA(launch_adjoint_step(d->v, args_at(t0+T, d->fi), j, true, d->stream), "adjoint objective");
+	}
+	auto reverse_states = [&](const uint64_t k0, const uint64_t k1, const void* start) -> int { // adjoint of steps k1-1 .. k0 from f^{k0} = start
+		EventTimer tr(d->stream);
+		FX3D_CUDA(cudaMemcpyAsync(segs(0), start, SB, cudaMemcpyDeviceToDevice, d->stream), "cudaMemcpyAsync(state)");
+		for(uint64_t k=k0; k+1ull<k1; k++) { const int r = step_out_of_place(d, segs(k-k0), segs(k-k0+1ull), t0+k); if(r!=LBM_OK) return r; }
+		recompute_ms += tr.stop(d->stream);
+		EventTimer ta(d->stream);
+		for(uint64_t k=k1; k-->k0;) {
+			j.state = segs(k-k0); j.obj_weight = in_window(t0+k) ? (float)weight : 0.0f;
+			FX3D_CUDA(launch_adjoint_step(d->v, args_at(t0+k, j.state), j, false, d->stream), "adjoint step");
+		}
+		adjoint_ms += ta.stop(d->stream);
+		return LBM_OK;
+	};
+	for(uint64_t s=nsnap; s-->0ull;) {
+		const uint64_t k0 = s*K, k1 = std::min<uint64_t>(k0+K, T);
+		if(levels==1u) { const int r = reverse_states(k0, k1, snap(s)); if(r!=LBM_OK) return r; continue; }
+		// two levels: sub-snapshots every K2 steps of the segment, then each sub-segment in reverse
+		EventTimer tr(d->stream);
+		FX3D_CUDA(cudaMemcpyAsync(subs(0), snap(s), SB, cudaMemcpyDeviceToDevice, d->stream), "cudaMemcpyAsync(sub-snapshot)");
+		FX3D_CUDA(cudaMemcpyAsync(segs(0), snap(s), SB, cudaMemcpyDeviceToDevice, d->stream), "cudaMemcpyAsync(state)");
+		for(uint64_t k=k0; k+1ull<k1; k++) {
+			void* a0 = segs((k-k0)%2ull); void* a1 = segs((k-k0+1ull)%2ull);
+			const int r = step_out_of_place(d, a0, a1, t0+k); if(r!=LBM_OK) return r;
+			if((k+1ull-k0)%K2==0ull) FX3D_CUDA(cudaMemcpyAsync(subs((k+1ull-k0)/K2), a1, SB, cudaMemcpyDeviceToDevice, d->stream), "cudaMemcpyAsync(sub-snapshot)");
+		}
+		recompute_ms += tr.stop(d->stream);
+		for(uint64_t b=(k1-k0+K2-1ull)/K2; b-->0ull;) {
+			const int r = reverse_states(k0+b*K2, std::min<uint64_t>(k0+(b+1ull)*K2, k1), subs(b));
+			if(r!=LBM_OK) return r;
+		}
+	}
+	double Jh = 0.0;
+	FX3D_CUDA(cudaMemcpyAsync(&Jh, Jd.p, sizeof(double), cudaMemcpyDeviceToHost, d->stream), "cudaMemcpyAsync(J)");
+	if(gradient) FX3D_CUDA(cudaMemcpyAsync(gradient, grad.p, N*12u, cudaMemcpyDeviceToHost, d->stream), "cudaMemcpyAsync(gradient)");
+	FX3D_CUDA(cudaStreamSynchronize(d->stream), "cudaStreamSynchronize");
+	{ const int r = check_kernel_error(d); if(r!=LBM_OK) return r; }
+	if(objective) *objective = Jh;
+	if(stats) {
+		stats->forward_ms = forward_ms; stats->recompute_ms = recompute_ms; stats->adjoint_ms = adjoint_ms;
+		stats->workspace_bytes = (uint64_t)need; stats->levels = levels; stats->reserved = 0u;
+	}
+	d->t_last_update_fields = UINT64_MAX;
+	d->t_last_force_field = UINT64_MAX;
+	return LBM_OK;
+}

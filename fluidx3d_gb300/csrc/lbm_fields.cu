@@ -8,6 +8,7 @@
 // accumulates a fixed, strided subset of cells in FP64 (warp shuffles, then shared memory) into its
 // own slot of a partials buffer, and one block adds the partials in a fixed order: the sum is FP64
 // and bit-reproducible from run to run.
+#include <mutex>
 #include "lbm_internal.h"
 #include "lbm_scheme.cuh"
 
@@ -15,12 +16,37 @@ namespace fx3d {
 
 constexpr int RB = 256; // threads per reduction block
 
-size_t rows_smem_bytes(const int q, const int storage, const uint32_t Nx) {
+RowPlan row_plan(const int q, const int storage, const uint32_t Nx, const uint32_t Ny, const uint32_t Nz) {
+	RowPlan p{0u, 0u, 0u};
 	const size_t elem = storage==ST_FP32 ? 4u : 2u;
-	const size_t rowbytes = (size_t)Nx*elem;
-	if(rowbytes%16u!=0u) return 0u; // bulk copies move whole 16-byte units from 16-byte-aligned addresses
-	const size_t smem = (size_t)q*((rowbytes+127u)&~(size_t)127u)+16u;
-	return smem<=200u*1024u ? smem : 0u;
+	if(Nx%16u!=0u) return p; // bulk copies move whole 16-byte units (the flags row is Nx bytes)
+	if((uint64_t)Ny*Nz>0xFFFFFFFFull) return p;
+	const size_t stride = (Nx*elem+127u)&~(size_t)127u;
+	const size_t stage = (size_t)q*stride+((Nx+127u)&~(size_t)127u);
+	const size_t budget2 = 112u*1024u, budget1 = 224u*1024u; // two CTAs per SM, or one
+	uint32_t s = 0u;
+	for(uint32_t k=4u; k>=2u && s==0u; k--) if(k*stage+128u<=budget2) s = k;
+	for(uint32_t k=4u; k>=2u && s==0u; k--) if(k*stage+128u<=budget1) s = k;
+	if(s==0u) return p;
+	p.stage_bytes = (uint32_t)stage; p.stages = s; p.smem = s*stage+128u;
+	return p;
+}
+
+int persistent_grid(const void* kernel, const int threads, const size_t smem) {
+	struct Entry { const void* k; int threads; size_t smem; int dev; int grid; };
+	static Entry cache[64];
+	static int count = 0;
+	static std::mutex m;
+	int dev = 0;
+	cudaGetDevice(&dev);
+	std::lock_guard<std::mutex> lock(m);
+	for(int i=0; i<count; i++) if(cache[i].k==kernel&&cache[i].threads==threads&&cache[i].smem==smem&&cache[i].dev==dev) return cache[i].grid;
+	int sms = 0, per_sm = 0;
+	cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
+	const int grid = sms*(per_sm>0 ? per_sm : 1);
+	if(count<64) cache[count++] = Entry{kernel, threads, smem, dev, grid};
+	return grid;
 }
 
 __device__ __forceinline__ double warp_sum(double v) {

@@ -19,12 +19,14 @@ struct Variant {
 	bool trt;     // false: SRT
 	int storage;  // ST_FP32 / ST_FP16S / ST_FP16C
 	int ext;      // EXT_* bits, normalised: FF only together with VF
+	bool fast;    // fast arithmetic (contracted, regrouped) instead of the reference's exact FP32 operation order
 };
 
 // arguments of one stream_collide / update_fields launch
 struct StepArgs {
 	GridDesc g;
-	void* fi;
+	void* fi;     // DDFs read by the step
+	void* fi_dst; // DDFs written by the step: fi (in place) or another array (row-staged path only)
 	float* rho;
 	float* u;
 	const uint8_t* flags;
@@ -32,16 +34,30 @@ struct StepArgs {
 	uint64_t t;
 	float fx, fy, fz, w;
 	int* err; // device error word (KERR_*), set by kernels whose bounded waits time out
+	// collision rates derived from w on the host with the reference's FP32 operations
+	// (src/kernel.cpp:1598, 1606-1609): 1-w, fma(w,-0.5,1), 0.5*w, 0.5*wm, fma(w,-0.25,0.5), fma(wm,-0.25,0.5)
+	float omw, c_tau, hp, hm, c_taup, c_taum;
 };
 
+// relaxation-rate constants of one domain (computed once on the host)
+struct Rates { float w, omw, c_tau, hp, hm, c_taup, c_taum; };
+Rates make_rates(float w);
+
 constexpr int BLOCK = 256;
-constexpr int ROW_TPB_MAX = 256; // threads per CTA of the row-staged stream_collide
+constexpr int ROW_TPB_MAX = 512; // threads per CTA of the row-staged stream_collide
 
 // stream_collide implementation: one thread per cell with direct global loads/stores ("cells"), or
 // one CTA per x-row with the row's slots staged in shared memory by bulk copies ("rows")
 enum : int { PATH_AUTO = 0, PATH_CELLS = 1, PATH_ROWS = 2 };
-// shared-memory bytes the row-staged kernel needs, 0 if the lattice does not fit its constraints
-size_t rows_smem_bytes(int q, int storage, uint32_t Nx);
+// shared-memory plan of the row-staged kernel: bytes of one stage (one x-row's Q DDF rows + its flags)
+// and the number of stages; stages==0 if the lattice does not fit its constraints
+struct RowPlan { uint32_t stage_bytes, stages; size_t smem; };
+RowPlan row_plan(int q, int storage, uint32_t Nx, uint32_t Ny, uint32_t Nz);
+inline size_t rows_smem_bytes(const int q, const int storage, const uint32_t Nx, const uint32_t Ny=1u, const uint32_t Nz=1u) {
+	return row_plan(q, storage, Nx, Ny, Nz).smem;
+}
+// persistent-grid size for a kernel: SMs x resident CTAs (cached per kernel, block size and smem)
+int persistent_grid(const void* kernel, int threads, size_t smem);
 
 // per-storage launchers (lbm_kernels_<storage>.cu)
 #define FX3D_DECLARE_LAUNCHERS(sfx) \

@@ -11,6 +11,7 @@
 #include "lbm_scheme.cuh"
 #include "lbm_internal.h"
 #include "lbm_bulk.cuh"
+#include "lbm_fast.cuh"
 
 namespace fx3d {
 
@@ -68,9 +69,24 @@ template<int Q, int EXT> __device__ __forceinline__ void cell_rho_u(const StepAr
 	shift_clamp<VF>(ux, uy, uz, rho, fx, fy, fz);
 }
 
-template<int Q, int ST, bool TRT, int EXT> __global__ void __launch_bounds__(BLOCK) k_stream_collide(const StepArgs a) {
+// one cell step on registers: f in, f out (exact: real units; fast: storage units)
+template<int Q, int ST, bool TRT, int EXT, bool FAST> __device__ __forceinline__ void cell_step(float* f, const StepArgs& a, const uint64_t n, const bool is_e) {
+	constexpr bool VF = (EXT&EXT_VF)!=0;
+	float rho, ux, uy, uz, fx, fy, fz;
+	if constexpr(FAST) {
+		float rm1, inv;
+		cell_rho_u_fast<Q, EXT, ST>(a, n, f, is_e, rho, rm1, inv, ux, uy, uz, fx, fy, fz);
+		collide_fast<Q, TRT, VF, ST>(f, rho, rm1, ux, uy, uz, fx, fy, fz, is_e, a);
+	} else {
+		cell_rho_u<Q, EXT>(a, n, f, is_e, rho, ux, uy, uz, fx, fy, fz);
+		collide<Q, TRT, VF>(f, rho, ux, uy, uz, fx, fy, fz, is_e, a);
+	}
+}
+template<int ST, bool FAST> using StepCodec = typename std::conditional<FAST, RawCodec<ST>, Codec<ST>>::type;
+
+template<int Q, int ST, bool TRT, int EXT, bool FAST> __global__ void __launch_bounds__(BLOCK) k_stream_collide(const StepArgs a) {
 	typedef typename Codec<ST>::T T;
-	constexpr bool VF = (EXT&EXT_VF)!=0, EQ = (EXT&EXT_EQ)!=0;
+	constexpr bool EQ = (EXT&EXT_EQ)!=0;
 	const Grid& g = grid_of(a.g);
 	CellPos c;
 	if(!cell_of_thread(g, c)) return;
@@ -81,45 +97,53 @@ template<int Q, int ST, bool TRT, int EXT> __global__ void __launch_bounds__(BLO
 	const Nbr nb(g, c.x, c.y, c.z);
 	const bool odd = (a.t&1ull)!=0ull;
 	float f[Q];
-	load_f<Q, ST>((const T*)a.fi, g.N, n, nb, odd, f);
+	load_f<Q, ST, StepCodec<ST, FAST>>((const T*)a.fi, g.N, n, nb, odd, f);
 	const bool is_e = EQ && flagsn_bo==TYPE_E;
-	float rho, ux, uy, uz, fx, fy, fz;
-	cell_rho_u<Q, EXT>(a, n, f, is_e, rho, ux, uy, uz, fx, fy, fz);
-	collide<Q, TRT, VF>(f, rho, ux, uy, uz, fx, fy, fz, is_e, a.w);
-	store_f<Q, ST>((T*)a.fi, g.N, n, nb, odd, f);
+	cell_step<Q, ST, TRT, EXT, FAST>(f, a, n, is_e);
+	store_f<Q, ST, StepCodec<ST, FAST>>((T*)a.fi, g.N, n, nb, odd, f);
 }
 
 // Row-staged stream_collide. At either parity the cells of one x-row (y,z) own exactly Q whole
 // rows of the DDF array: row (y,z) of array 0 and of the arrays of their "own" slots, and for each
 // pair (i,i+1) row (y+c_iy, z+c_iz) of the array of their neighbour slots, rotated by c_ix
-// (periodic in x). One CTA per x-row bulk-loads those Q rows into shared memory (cp.async.bulk,
-// completion on one mbarrier), collides every cell of the row from shared memory and bulk-stores
-// the same Q rows back. Every global access is a whole 16-byte-aligned row, no data in flight sits
-// in registers, and slots of solid cells go back unchanged. Rows are owned by exactly one CTA per
-// parity, so CTAs never touch each other's rows.
-template<int Q, int ST> struct RowLayout {
-	typedef typename Codec<ST>::T T;
-	uint32_t rowbytes, stride; // bytes of one row, and its 128-byte-aligned pitch in shared memory
-	__host__ __device__ explicit RowLayout(const uint32_t Nx) : rowbytes(Nx*(uint32_t)sizeof(T)), stride((Nx*(uint32_t)sizeof(T)+127u)&~127u) {}
-	__host__ __device__ size_t smem_bytes() const { return (size_t)Q*stride+16u; }
+// (periodic in x). Rows are owned by exactly one x-row per parity, so x-rows never touch each
+// other's DDF rows, and a whole x-row can be moved with Q aligned bulk copies.
+//
+// Persistent CTAs walk x-rows r = blockIdx.x + j*gridDim.x through a ring of `stages` shared-memory
+// stages (one x-row's Q DDF rows + its flags row each): while x-row j is collided from shared memory,
+// the bulk loads (cp.async.bulk, completion on the stage's mbarrier) of x-rows j+1..j+P are in flight
+// and the bulk stores of x-row j-1 drain. Every global access is a whole 16-byte-aligned row and no
+// data in flight occupies registers. Slots of solid cells go back unchanged, so the step may also
+// write to a different array than it reads (fi_dst), which the adjoint's recomputation uses.
+struct RowStageLayout {
+	uint32_t rowbytes, stride, flags_off, stage_bytes;
+	__host__ __device__ RowStageLayout(const int q, const uint32_t elem, const uint32_t Nx) {
+		rowbytes = Nx*elem; stride = (rowbytes+127u)&~127u;
+		flags_off = (uint32_t)q*stride; stage_bytes = flags_off+((Nx+127u)&~127u);
+	}
 };
 
-template<int Q, int ST, bool TRT, int EXT> __global__ void __launch_bounds__(ROW_TPB_MAX) k_stream_collide_rows(const StepArgs a) {
+template<int Q, int ST, bool TRT, int EXT, bool FAST> __global__ void __launch_bounds__(ROW_TPB_MAX, (Q==19 ? 2 : 1))
+k_stream_collide_rows(const StepArgs a, const uint32_t stages) {
 	typedef typename Codec<ST>::T T;
-	constexpr bool VF = (EXT&EXT_VF)!=0, EQ = (EXT&EXT_EQ)!=0;
+	typedef StepCodec<ST, FAST> CD;
+	constexpr bool EQ = (EXT&EXT_EQ)!=0;
 	extern __shared__ __align__(128) unsigned char smem[];
+	__shared__ int abort_rows;
 	const Grid& g = grid_of(a.g);
-	const uint32_t Nx = g.Nx, Ny = g.Ny, Nz = g.Nz, y = blockIdx.x, z = blockIdx.y;
-	const RowLayout<Q, ST> L(Nx);
-	uint64_t* bar = reinterpret_cast<uint64_t*>(smem+(size_t)Q*L.stride);
-	auto srow = [&](const int s) { return reinterpret_cast<T*>(smem+(size_t)s*L.stride); };
+	const uint32_t Nx = g.Nx, Ny = g.Ny, Nz = g.Nz, rows = Ny*Nz, tid = threadIdx.x;
+	const RowStageLayout L(Q, (uint32_t)sizeof(T), Nx);
+	uint64_t* bars = reinterpret_cast<uint64_t*>(smem);
+	unsigned char* stage0 = smem+128;
 	const bool odd = (a.t&1ull)!=0ull;
 	const uint64_t N = g.N;
-	const uint64_t row0 = ((uint64_t)z*Ny+y)*Nx;
-	T* fi = (T*)a.fi;
-	// global start of the row held in shared-memory slot s (0; i: own slot; i+1: neighbour slot)
-	auto grow = [&](auto ic) -> uint64_t {
+	const T* src = (const T*)a.fi;
+	T* dst = (T*)a.fi_dst;
+	const uint32_t P = stages>2u ? stages-2u : 1u; // x-rows loaded ahead of the one being collided
+	// global start of DDF slot row s of x-row (y,z): 0; i (odd): own slot; i+1: neighbour slot
+	auto grow = [&](auto ic, const uint32_t y, const uint32_t z) -> uint64_t {
 		constexpr int s = decltype(ic)::value;
+		const uint64_t row0 = ((uint64_t)z*Ny+y)*Nx;
 		if constexpr(s==0) return row0;
 		else if constexpr(s%2==1) return (uint64_t)(odd ? s : s+1)*N+row0;
 		else {
@@ -129,53 +153,83 @@ template<int Q, int ST, bool TRT, int EXT> __global__ void __launch_bounds__(ROW
 			return (uint64_t)(odd ? i+1 : i)*N+((uint64_t)zz*Ny+yy)*Nx;
 		}
 	};
-	if(threadIdx.x==0u) {
-		mbar_init(bar, 1u);
+	auto issue_loads = [&](const uint32_t r, const uint32_t s) { // thread 0 only
+		const uint32_t z = r/Ny, y = r-z*Ny;
+		unsigned char* st = stage0+(size_t)s*L.stage_bytes;
+		uint64_t* bar = bars+s;
+		mbar_arrive_expect_tx(bar, (uint32_t)Q*L.rowbytes+Nx);
+		Unroll<0, Q, 1>::run([&](auto ic) { bulk_load(st+(size_t)decltype(ic)::value*L.stride, src+grow(ic, y, z), L.rowbytes, bar); });
+		bulk_load(st+L.flags_off, a.flags+((uint64_t)z*Ny+y)*Nx, Nx, bar);
+	};
+	if(tid==0u) {
+		for(uint32_t s=0u; s<stages; s++) mbar_init(bars+s, 1u);
 		fence_mbar_init();
-		mbar_arrive_expect_tx(bar, (uint32_t)Q*L.rowbytes);
-		Unroll<0, Q, 1>::run([&](auto ic) { bulk_load(srow(decltype(ic)::value), fi+grow(ic), L.rowbytes, bar); });
+		abort_rows = 0;
+		for(uint32_t p=0u; p<P; p++) { const uint64_t r = (uint64_t)blockIdx.x+(uint64_t)p*gridDim.x; if(r<rows) issue_loads((uint32_t)r, p); }
 	}
 	__syncthreads();
-	if(!mbar_wait_bounded(bar, 0u, a.err)) {
-		mbar_wait_bounded(bar, 0u, nullptr); // give copies still in flight a second bounded chance, then leave the row untouched
-		return;
+	uint32_t j = 0u;
+	for(uint64_t r=blockIdx.x; r<rows; r+=gridDim.x, j++) {
+		const uint32_t s = j%stages;
+		if(tid==0u) {
+			const uint64_t rn = r+(uint64_t)P*gridDim.x;
+			if(rn<rows) {
+				// the stage of x-row j+P last held x-row j+P-stages: its stores must have left shared memory
+				if(stages-P-1u>=1u) bulk_wait_read_but1(); else bulk_wait_read_all();
+				issue_loads((uint32_t)rn, (j+P)%stages);
+			}
+		}
+		const bool ok = mbar_wait_bounded(bars+s, (j/stages)&1u, a.err);
+		if(!ok) abort_rows = 1;
+		unsigned char* st = stage0+(size_t)s*L.stage_bytes;
+		auto srow = [&](const int k) { return reinterpret_cast<T*>(st+(size_t)k*L.stride); };
+		const uint8_t* fl = st+L.flags_off;
+		const uint32_t z = (uint32_t)(r/Ny), y = (uint32_t)(r-(uint64_t)z*Ny);
+		const uint64_t row0 = ((uint64_t)z*Ny+y)*Nx;
+		for(uint32_t x=tid; ok && x<Nx; x+=blockDim.x) {
+			const uint8_t flagsn = fl[x];
+			const uint8_t flagsn_bo = flagsn&TYPE_BO;
+			if(flagsn_bo==TYPE_S||(flagsn&TYPE_SU)==TYPE_G) continue;
+			const uint32_t xp = x+1u==Nx ? 0u : x+1u, xm = x==0u ? Nx-1u : x-1u;
+			float f[Q];
+			f[0] = CD::decode(srow(0)[x]);
+			Unroll<1, Q, 2>::run([&](auto ic) {
+				constexpr int i = decltype(ic)::value, cx = vs_c(0, i);
+				const uint32_t xi = cx>0 ? xp : cx<0 ? xm : x;
+				f[i] = CD::decode(srow(i)[x]);
+				f[i+1] = CD::decode(srow(i+1)[xi]);
+			});
+			const bool is_e = EQ && flagsn_bo==TYPE_E;
+			cell_step<Q, ST, TRT, EXT, FAST>(f, a, row0+x, is_e);
+			srow(0)[x] = CD::encode(f[0]);
+			Unroll<1, Q, 2>::run([&](auto ic) {
+				constexpr int i = decltype(ic)::value, cx = vs_c(0, i);
+				const uint32_t xi = cx>0 ? xp : cx<0 ? xm : x;
+				srow(i+1)[xi] = CD::encode(f[i]);
+				srow(i)[x] = CD::encode(f[i+1]);
+			});
+		}
+		fence_proxy_async_smem();
+		__syncthreads();
+		if(abort_rows) { // a bounded wait ran out: store nothing more, drain the copies still in flight
+			if(tid==0u) {
+				for(uint32_t p=0u; p<=P; p++) {
+					const uint64_t rp = r+(uint64_t)p*gridDim.x;
+					if(rp<rows) mbar_wait_bounded(bars+(j+p)%stages, ((j+p)/stages)&1u, nullptr);
+				}
+				bulk_wait_all();
+			}
+			return;
+		}
+		if(tid==0u) {
+			Unroll<0, Q, 1>::run([&](auto ic) { bulk_store(dst+grow(ic, y, z), st+(size_t)decltype(ic)::value*L.stride, L.rowbytes); });
+			bulk_commit();
+		}
 	}
-	for(uint32_t x=threadIdx.x; x<Nx; x+=blockDim.x) {
-		const uint64_t n = row0+x;
-		const uint8_t flagsn = a.flags[n];
-		const uint8_t flagsn_bo = flagsn&TYPE_BO;
-		if(flagsn_bo==TYPE_S||(flagsn&TYPE_SU)==TYPE_G) continue;
-		const uint32_t xp = x+1u==Nx ? 0u : x+1u, xm = x==0u ? Nx-1u : x-1u;
-		float f[Q];
-		f[0] = Codec<ST>::decode(srow(0)[x]);
-		Unroll<1, Q, 2>::run([&](auto ic) {
-			constexpr int i = decltype(ic)::value, cx = vs_c(0, i);
-			const uint32_t xi = cx>0 ? xp : cx<0 ? xm : x;
-			f[i] = Codec<ST>::decode(srow(i)[x]);
-			f[i+1] = Codec<ST>::decode(srow(i+1)[xi]);
-		});
-		const bool is_e = EQ && flagsn_bo==TYPE_E;
-		float rho, ux, uy, uz, fx, fy, fz;
-		cell_rho_u<Q, EXT>(a, n, f, is_e, rho, ux, uy, uz, fx, fy, fz);
-		collide<Q, TRT, VF>(f, rho, ux, uy, uz, fx, fy, fz, is_e, a.w);
-		srow(0)[x] = Codec<ST>::encode(f[0]);
-		Unroll<1, Q, 2>::run([&](auto ic) {
-			constexpr int i = decltype(ic)::value, cx = vs_c(0, i);
-			const uint32_t xi = cx>0 ? xp : cx<0 ? xm : x;
-			srow(i+1)[xi] = Codec<ST>::encode(f[i]);
-			srow(i)[x] = Codec<ST>::encode(f[i+1]);
-		});
-	}
-	fence_proxy_async_smem();
-	__syncthreads();
-	if(threadIdx.x==0u) {
-		Unroll<0, Q, 1>::run([&](auto ic) { bulk_store(fi+grow(ic), srow(decltype(ic)::value), L.rowbytes); });
-		bulk_commit();
-		bulk_wait_read_all(); // shared memory must outlive the reads of the stores
-	}
+	if(tid==0u) bulk_wait_all(); // stores complete before the CTA (and its shared memory) goes away
 }
 
-template<int Q, int ST, int EXT> __global__ void __launch_bounds__(BLOCK) k_update_fields(const StepArgs a) {
+template<int Q, int ST, int EXT, bool FAST> __global__ void __launch_bounds__(BLOCK) k_update_fields(const StepArgs a) {
 	typedef typename Codec<ST>::T T;
 	constexpr bool EQ = (EXT&EXT_EQ)!=0;
 	const Grid& g = grid_of(a.g);
@@ -188,9 +242,15 @@ template<int Q, int ST, int EXT> __global__ void __launch_bounds__(BLOCK) k_upda
 	if(EQ && flagsn_bo==TYPE_E) return; // preset rho/u of TYPE_E cells are kept
 	const Nbr nb(g, c.x, c.y, c.z);
 	float f[Q];
-	load_f<Q, ST>((const T*)a.fi, N, n, nb, (a.t&1ull)!=0ull, f);
+	load_f<Q, ST, StepCodec<ST, FAST>>((const T*)a.fi, N, n, nb, (a.t&1ull)!=0ull, f);
 	float rho, ux, uy, uz, fx, fy, fz;
-	cell_rho_u<Q, EXT&~EXT_EQ>(a, n, f, false, rho, ux, uy, uz, fx, fy, fz);
+	if constexpr(FAST) {
+		float rm1, inv;
+		cell_rho_u_fast<Q, EXT&~EXT_EQ, ST>(a, n, f, false, rho, rm1, inv, ux, uy, uz, fx, fy, fz);
+		rho *= 1.0f/RawCodec<ST>::K; // R = K*rho, K a power of two
+	} else {
+		cell_rho_u<Q, EXT&~EXT_EQ>(a, n, f, false, rho, ux, uy, uz, fx, fy, fz);
+	}
 	a.rho[n] = rho; a.u[n] = ux; a.u[N+n] = uy; a.u[2ull*N+n] = uz;
 }
 
@@ -214,57 +274,66 @@ template<int Q, int ST> __global__ void __launch_bounds__(BLOCK) k_update_force_
 // ---------------------------------------------------------------- dispatch
 inline dim3 cell_grid(const GridDesc& g) { return dim3((g.NxNy+BLOCK-1u)/BLOCK, g.Nz, 1u); }
 
-template<int ST, int Q, bool TRT, int EXT> inline cudaError_t sc_launch(const StepArgs& a, const bool rows, cudaStream_t s) {
+template<int ST, int Q, bool TRT, int EXT, bool FAST> inline cudaError_t sc_launch_t(const StepArgs& a, const bool rows, cudaStream_t s) {
 	if(rows) {
-		const RowLayout<Q, ST> L(a.g.Nx);
-		const size_t smem = L.smem_bytes();
-		if(smem>48u*1024u) { // opt in to more than 48 KB of dynamic shared memory (per device, so on every such launch)
-			const cudaError_t e = cudaFuncSetAttribute(k_stream_collide_rows<Q, ST, TRT, EXT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+		const RowPlan plan = row_plan(Q, ST, a.g.Nx, a.g.Ny, a.g.Nz);
+		if(plan.stages==0u) return cudaErrorInvalidConfiguration;
+		auto kernel = k_stream_collide_rows<Q, ST, TRT, EXT, FAST>;
+		if(plan.smem>48u*1024u) { // opt in to more than 48 KB of dynamic shared memory (per device, so on every such launch)
+			const cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)plan.smem);
 			if(e!=cudaSuccess) return e;
 		}
-		const uint32_t tpb = a.g.Nx>=(uint32_t)ROW_TPB_MAX ? (uint32_t)ROW_TPB_MAX : (a.g.Nx+31u)&~31u;
-		k_stream_collide_rows<Q, ST, TRT, EXT><<<dim3(a.g.Ny, a.g.Nz, 1u), tpb, smem, s>>>(a);
+		const int tpb = a.g.Nx>=(uint32_t)ROW_TPB_MAX ? ROW_TPB_MAX : (int)((a.g.Nx+31u)&~31u);
+		const uint64_t rows_total = (uint64_t)a.g.Ny*a.g.Nz;
+		int grid = persistent_grid((const void*)kernel, tpb, plan.smem);
+		if((uint64_t)grid>rows_total) grid = (int)rows_total;
+		kernel<<<grid, tpb, plan.smem, s>>>(a, plan.stages);
 	} else {
-		k_stream_collide<Q, ST, TRT, EXT><<<cell_grid(a.g), BLOCK, 0, s>>>(a);
+		if(a.fi_dst!=a.fi) return cudaErrorInvalidValue; // one thread per cell steps in place only
+		k_stream_collide<Q, ST, TRT, EXT, FAST><<<cell_grid(a.g), BLOCK, 0, s>>>(a);
 	}
 	return cudaGetLastError();
 }
-template<int ST, int Q, bool TRT> inline cudaError_t sc_ext(const int ext, const StepArgs& a, const bool rows, cudaStream_t s) {
+template<int ST, int Q, bool TRT, int EXT> inline cudaError_t sc_launch(const StepArgs& a, const bool rows, const bool fast, cudaStream_t s) {
+	return fast ? sc_launch_t<ST, Q, TRT, EXT, true>(a, rows, s) : sc_launch_t<ST, Q, TRT, EXT, false>(a, rows, s);
+}
+template<int ST, int Q, bool TRT> inline cudaError_t sc_ext(const int ext, const StepArgs& a, const bool rows, const bool fast, cudaStream_t s) {
 	switch(ext) {
-		case 0:                        return sc_launch<ST, Q, TRT, 0>(a, rows, s);
-		case EXT_VF:                   return sc_launch<ST, Q, TRT, EXT_VF>(a, rows, s);
-		case EXT_VF|EXT_FF:            return sc_launch<ST, Q, TRT, EXT_VF|EXT_FF>(a, rows, s);
-		case EXT_EQ:                   return sc_launch<ST, Q, TRT, EXT_EQ>(a, rows, s);
-		case EXT_EQ|EXT_VF:            return sc_launch<ST, Q, TRT, EXT_EQ|EXT_VF>(a, rows, s);
-		case EXT_EQ|EXT_VF|EXT_FF:     return sc_launch<ST, Q, TRT, EXT_EQ|EXT_VF|EXT_FF>(a, rows, s);
+		case 0:                        return sc_launch<ST, Q, TRT, 0>(a, rows, fast, s);
+		case EXT_VF:                   return sc_launch<ST, Q, TRT, EXT_VF>(a, rows, fast, s);
+		case EXT_VF|EXT_FF:            return sc_launch<ST, Q, TRT, EXT_VF|EXT_FF>(a, rows, fast, s);
+		case EXT_EQ:                   return sc_launch<ST, Q, TRT, EXT_EQ>(a, rows, fast, s);
+		case EXT_EQ|EXT_VF:            return sc_launch<ST, Q, TRT, EXT_EQ|EXT_VF>(a, rows, fast, s);
+		case EXT_EQ|EXT_VF|EXT_FF:     return sc_launch<ST, Q, TRT, EXT_EQ|EXT_VF|EXT_FF>(a, rows, fast, s);
 		default: return cudaErrorInvalidValue;
 	}
 }
 template<int ST> cudaError_t launch_stream_collide_t(const Variant& v, const StepArgs& a, const int path, cudaStream_t s) {
-	const bool rows_ok = rows_smem_bytes(v.q, ST, a.g.Nx)!=0u;
+	const bool rows_ok = row_plan(v.q, ST, a.g.Nx, a.g.Ny, a.g.Nz).stages!=0u;
 	if(path==PATH_ROWS && !rows_ok) return cudaErrorInvalidConfiguration;
 	const bool rows = path==PATH_ROWS || (path==PATH_AUTO && rows_ok);
-	if(v.q==19) return v.trt ? sc_ext<ST, 19, true>(v.ext, a, rows, s) : sc_ext<ST, 19, false>(v.ext, a, rows, s);
-	if(v.q==27) return v.trt ? sc_ext<ST, 27, true>(v.ext, a, rows, s) : sc_ext<ST, 27, false>(v.ext, a, rows, s);
+	if(v.q==19) return v.trt ? sc_ext<ST, 19, true>(v.ext, a, rows, v.fast, s) : sc_ext<ST, 19, false>(v.ext, a, rows, v.fast, s);
+	if(v.q==27) return v.trt ? sc_ext<ST, 27, true>(v.ext, a, rows, v.fast, s) : sc_ext<ST, 27, false>(v.ext, a, rows, v.fast, s);
 	return cudaErrorInvalidValue;
 }
 
-template<int ST, int Q, int EXT> inline void uf_launch(const StepArgs& a, cudaStream_t s) {
-	k_update_fields<Q, ST, EXT><<<cell_grid(a.g), BLOCK, 0, s>>>(a);
+template<int ST, int Q, int EXT> inline void uf_launch(const StepArgs& a, const bool fast, cudaStream_t s) {
+	if(fast) k_update_fields<Q, ST, EXT, true><<<cell_grid(a.g), BLOCK, 0, s>>>(a);
+	else k_update_fields<Q, ST, EXT, false><<<cell_grid(a.g), BLOCK, 0, s>>>(a);
 }
-template<int ST, int Q> inline bool uf_ext(const int ext, const StepArgs& a, cudaStream_t s) {
+template<int ST, int Q> inline bool uf_ext(const int ext, const StepArgs& a, const bool fast, cudaStream_t s) {
 	switch(ext) {
-		case 0:                        uf_launch<ST, Q, 0>(a, s); return true;
-		case EXT_VF:                   uf_launch<ST, Q, EXT_VF>(a, s); return true;
-		case EXT_VF|EXT_FF:            uf_launch<ST, Q, EXT_VF|EXT_FF>(a, s); return true;
-		case EXT_EQ:                   uf_launch<ST, Q, EXT_EQ>(a, s); return true;
-		case EXT_EQ|EXT_VF:            uf_launch<ST, Q, EXT_EQ|EXT_VF>(a, s); return true;
-		case EXT_EQ|EXT_VF|EXT_FF:     uf_launch<ST, Q, EXT_EQ|EXT_VF|EXT_FF>(a, s); return true;
+		case 0:                        uf_launch<ST, Q, 0>(a, fast, s); return true;
+		case EXT_VF:                   uf_launch<ST, Q, EXT_VF>(a, fast, s); return true;
+		case EXT_VF|EXT_FF:            uf_launch<ST, Q, EXT_VF|EXT_FF>(a, fast, s); return true;
+		case EXT_EQ:                   uf_launch<ST, Q, EXT_EQ>(a, fast, s); return true;
+		case EXT_EQ|EXT_VF:            uf_launch<ST, Q, EXT_EQ|EXT_VF>(a, fast, s); return true;
+		case EXT_EQ|EXT_VF|EXT_FF:     uf_launch<ST, Q, EXT_EQ|EXT_VF|EXT_FF>(a, fast, s); return true;
 		default: return false;
 	}
 }
 template<int ST> cudaError_t launch_update_fields_t(const Variant& v, const StepArgs& a, cudaStream_t s) {
-	const bool ok = v.q==19 ? uf_ext<ST, 19>(v.ext, a, s) : v.q==27 ? uf_ext<ST, 27>(v.ext, a, s) : false;
+	const bool ok = v.q==19 ? uf_ext<ST, 19>(v.ext, a, v.fast, s) : v.q==27 ? uf_ext<ST, 27>(v.ext, a, v.fast, s) : false;
 	return ok ? cudaGetLastError() : cudaErrorInvalidValue;
 }
 

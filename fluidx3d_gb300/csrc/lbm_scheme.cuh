@@ -2,10 +2,11 @@
 // addressing, moments, equilibrium, Guo forcing and the SRT/TRT collision, written so every kernel
 // of the library (forward, fields, forces, adjoint) shares one definition of the arithmetic.
 //
-// Arithmetic contract: FP32, the reference's operation order, fmaf() exactly where the reference
-// writes fma() (src/kernel.cpp:1004-1101, 1550-1633) and no other contraction -- the library is
-// compiled with -fmad=false -prec-div=true -ftz=false -- so a kernel's result is bit-identical to the
-// FP32 restatement of the scheme on the CPU.
+// Arithmetic contract of this file ("exact" mode): FP32 in the reference's operation order, fmaf()
+// exactly where the reference writes fma() (src/kernel.cpp:1004-1101, 1550-1633) and every other
+// multiply/add/divide spelled as a rounding intrinsic (__fmul_rn, __fadd_rn, __fdiv_rn), which the
+// compiler never contracts, so a kernel's result is bit-identical to the FP32 restatement of the
+// scheme on the CPU. The fast mode (lbm_fast.cuh) trades that for about a third of the instructions.
 #pragma once
 #include <cuda_fp16.h>
 #include <stdint.h>
@@ -120,24 +121,24 @@ template<int I, int END, int STEP> struct Unroll {
 // ---------------------------------------------------------------- Esoteric-Pull (src/kernel.cpp:1326-1339)
 // Pair (i,i+1), i odd: slot A = (n, odd ? i : i+1), slot B = (j[i], odd ? i+1 : i). Load reads
 // f_i from A and f_{i+1} from B; store writes f_i to B and f_{i+1} to A.
-template<int Q, int ST> __device__ __forceinline__ void load_f(const typename Codec<ST>::T* fi, const uint64_t N, const uint64_t n, const Nbr& nb,
-                                                              const bool odd, float* f) {
+template<int Q, int ST, class CD=Codec<ST>> __device__ __forceinline__ void load_f(const typename Codec<ST>::T* fi, const uint64_t N, const uint64_t n, const Nbr& nb,
+                                                                                  const bool odd, float* f) {
 	const uint64_t e = odd ? 0ull : N;
-	f[0] = Codec<ST>::load(fi+n);
+	f[0] = CD::decode(fi[n]);
 	Unroll<1, Q, 2>::run([&](auto ic) {
 		constexpr int i = decltype(ic)::value;
-		f[i   ] = Codec<ST>::load(fi+((uint64_t)i*N+e+n));
-		f[i+1] = Codec<ST>::load(fi+((uint64_t)(i+1)*N-e+nb.template j<i>()));
+		f[i   ] = CD::decode(fi[(uint64_t)i*N+e+n]);
+		f[i+1] = CD::decode(fi[(uint64_t)(i+1)*N-e+nb.template j<i>()]);
 	});
 }
-template<int Q, int ST> __device__ __forceinline__ void store_f(typename Codec<ST>::T* fi, const uint64_t N, const uint64_t n, const Nbr& nb,
-                                                               const bool odd, const float* f) {
+template<int Q, int ST, class CD=Codec<ST>> __device__ __forceinline__ void store_f(typename Codec<ST>::T* fi, const uint64_t N, const uint64_t n, const Nbr& nb,
+                                                                                   const bool odd, const float* f) {
 	const uint64_t e = odd ? 0ull : N;
-	Codec<ST>::store(fi+n, f[0]);
+	fi[n] = CD::encode(f[0]);
 	Unroll<1, Q, 2>::run([&](auto ic) {
 		constexpr int i = decltype(ic)::value;
-		Codec<ST>::store(fi+((uint64_t)(i+1)*N-e+nb.template j<i>()), f[i]);
-		Codec<ST>::store(fi+((uint64_t)i*N+e+n), f[i+1]);
+		fi[(uint64_t)(i+1)*N-e+nb.template j<i>()] = CD::encode(f[i]);
+		fi[(uint64_t)i*N+e+n] = CD::encode(f[i+1]);
 	});
 }
 
@@ -208,12 +209,12 @@ template<bool VF> __device__ __forceinline__ void shift_clamp(float& ux, float& 
 // SRT / TRT collision of all directions in place (src/kernel.cpp:1595-1633). f: streamed DDFs,
 // rho/u: after force shift and clamp, fx..fz: total force, is_e: TYPE_E cell (f = feq).
 template<int Q, bool TRT, bool VF> __device__ __forceinline__ void collide(float* f, const float rho, const float ux, const float uy, const float uz,
-                                                                          const float fx, const float fy, const float fz, const bool is_e, const float w) {
+                                                                          const float fx, const float fy, const float fz, const bool is_e, const StepArgs& a) {
+	const float w = a.w;
 	const EqState s = eq_state(rho, ux, uy, uz);
 	const float uF = VF ? forcing_uF(ux, uy, uz, fx, fy, fz) : 0.0f;
 	if constexpr(!TRT) {
-		const float omw = __fsub_rn(1.0f, w);
-		const float c_tau = VF ? fmaf(w, -0.5f, 1.0f) : 0.0f;
+		const float omw = a.omw, c_tau = a.c_tau;
 		{
 			const float fe = feq0<Q>(s);
 			const float Fi = VF ? __fmul_rn(forcing_term<Q, 0>(ux, uy, uz, fx, fy, fz, uF), c_tau) : 0.0f;
@@ -229,10 +230,7 @@ template<int Q, bool TRT, bool VF> __device__ __forceinline__ void collide(float
 			f[i+1] = is_e ? fb : fmaf(omw, f[i+1], fmaf(w, fb, Fb));
 		});
 	} else {
-		const float wp = w;
-		const float wm = __fdiv_rn(1.0f, __fadd_rn(__fdiv_rn(0.1875f, __fsub_rn(__fdiv_rn(1.0f, w), 0.5f)), 0.5f));
-		const float hp = __fmul_rn(0.5f, wp), hm = __fmul_rn(0.5f, wm);
-		const float c_taup = VF ? fmaf(wp, -0.25f, 0.5f) : 0.0f, c_taum = VF ? fmaf(wm, -0.25f, 0.5f) : 0.0f;
+		const float hp = a.hp, hm = a.hm, c_taup = a.c_taup, c_taum = a.c_taum; // host-computed with the reference's operations
 		{ // i = 0: its own opposite
 			const float fe = feq0<Q>(s);
 			float Fi = 0.0f;

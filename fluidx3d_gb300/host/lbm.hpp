@@ -4,7 +4,8 @@
 //
 // The variant is chosen the way the reference chooses it, with macros defined before this header
 // is included (src/defines.hpp:5-29): D3Q19 (default) or D3Q27; SRT (default) or TRT; FP16S or
-// FP16C DDF storage (default FP32); VOLUME_FORCE, FORCE_FIELD, EQUILIBRIUM_BOUNDARIES.
+// FP16C DDF storage (default FP32); VOLUME_FORCE, FORCE_FIELD, EQUILIBRIUM_BOUNDARIES; and, new here,
+// EXACT_ARITHMETIC / FAST_ARITHMETIC (default: exact with FP32 storage, fast with FP16S/FP16C).
 //
 // Errors: the reference prints and exits (src/utilities.hpp:4159-4166); here a failed call throws
 // lbm_error carrying the C-ABI status and message (uncaught, it ends the program the same way).
@@ -136,6 +137,13 @@ inline lbm_config lbm_config_from_defines(const uint Nx, const uint Ny, const ui
 #endif
 	c.device = -1;
 	c.nu = nu; c.fx = fx; c.fy = fy; c.fz = fz;
+#if defined(EXACT_ARITHMETIC)
+	c.arithmetic = LBM_ARITH_EXACT; // the reference's FP32 operation order, bit for bit
+#elif defined(FAST_ARITHMETIC)
+	c.arithmetic = LBM_ARITH_FAST;
+#else
+	c.arithmetic = LBM_ARITH_AUTO;  // exact with FP32 storage, fast with FP16S/FP16C
+#endif
 	return c;
 }
 

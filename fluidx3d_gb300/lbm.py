@@ -12,6 +12,9 @@ Usage follows the reference's setups (src/setup.cpp):
 
 The reference picks the velocity set, collision operator, DDF storage and extensions with
 #defines in src/defines.hpp; here they are constructor keywords with the same meaning.
+``arithmetic="exact"`` evaluates the reference's FP32 operation order bit for bit, ``"fast"``
+contracts multiply-adds and regroups terms (agreeing to FP32 rounding); the default ``"auto"`` is
+exact with FP32 DDF storage and fast with FP16S/FP16C storage.
 """
 from __future__ import annotations
 
@@ -76,9 +79,11 @@ class LBM:
     """One LBM domain on one GPU with the reference's LBM interface."""
 
     def __init__(self, Nx, Ny, Nz, nu, fx=0.0, fy=0.0, fz=0.0, *, velocity_set=19, collision="srt", storage="fp32",
-                 extensions=(), device=-1):
+                 extensions=(), device=-1, arithmetic="auto"):
         self.config = C.LBMConfig(int(Nx), int(Ny), int(Nz), int(velocity_set), C.COLLISIONS[collision], C.STORAGES[storage],
-                                  _ext_bits(extensions), int(device), float(nu), float(fx), float(fy), float(fz))
+                                  _ext_bits(extensions), int(device), float(nu), float(fx), float(fy), float(fz),
+                                  C.ARITHMETICS[arithmetic])
+        self.arithmetic = arithmetic
         self.velocity_set, self.collision, self.storage = int(velocity_set), collision, storage
         self.extensions = tuple(extensions)
         L = C.load()
@@ -167,6 +172,26 @@ class LBM:
         cx, cy, cz = (float(v) for v in rotation_center)
         self._check(C.load().lbm_object_torque(self._d, flag_marker, cx, cy, cz, out))
         return np.array(out[:3])
+
+    # ------------------------------------------------------------------ adjoint (new; no reference counterpart)
+    def run_adjoint(self, steps, objective="ke_plane", window=None, plane_x=0, marker=TYPE_S, checkpoint_interval=100):
+        """Runs `steps` forward time steps (like run) and the checkpointed discrete adjoint back through
+        them. Returns (J, dJ/dF, stats): J the objective averaged over the states after the time steps
+        of `window` (inclusive, absolute), dJ/dF as a 3N SoA float32 array. F (the per-cell force field,
+        FORCE_FIELD) is the design variable; the domain ends at the forward state, t advanced by steps."""
+        if not self.initialized:
+            self.initialize()
+        t0 = self.get_t()
+        if window is None:
+            window = (t0 + steps, t0 + steps)
+        cfg = C.AdjointConfig(int(steps), int(checkpoint_interval), C.OBJECTIVES[objective], int(plane_x), int(marker), 0,
+                              int(window[0]), int(window[1]))
+        J = ctypes.c_double()
+        grad = np.empty(3 * self.get_N(), np.float32)
+        st = C.AdjointStats()
+        self._check(C.load().lbm_run_adjoint(self._d, ctypes.byref(cfg), ctypes.byref(J), grad.ctypes.data, ctypes.byref(st)))
+        stats = {k: getattr(st, k) for k, _ in C.AdjointStats._fields_ if k != "reserved"}
+        return J.value, grad, stats
 
     # ------------------------------------------------------------------ geometry (src/lbm.cpp:1074-1093)
     def voxelize_mesh_on_device(self, mesh, flag=TYPE_S, rotation_center=(0.0, 0.0, 0.0), linear_velocity=(0.0, 0.0, 0.0),

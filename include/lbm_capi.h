@@ -47,6 +47,12 @@ enum {
 	LBM_EXT_FORCE_FIELD = 2,           /* FORCE_FIELD: per-cell force F added to (fx,fy,fz) */
 	LBM_EXT_EQUILIBRIUM_BOUNDARIES = 4 /* EQUILIBRIUM_BOUNDARIES: TYPE_E cells held at their rho/u */
 };
+/* arithmetic of the collision. EXACT evaluates the reference's FP32 operation order with IEEE
+ * rounding at every step: bit-identical to the reference's kernel text evaluated on a CPU. FAST
+ * contracts multiply-adds and regroups terms the way the reference's own GPU build may
+ * (-cl-mad-enable); it agrees with EXACT to FP32 rounding. AUTO (default) is EXACT for FP32 DDF
+ * storage and FAST for FP16S/FP16C, where the 16-bit storage rounding dominates either error. */
+enum { LBM_ARITH_AUTO = 0, LBM_ARITH_EXACT = 1, LBM_ARITH_FAST = 2 };
 enum { LBM_FIELD_RHO = 0, LBM_FIELD_U = 1, LBM_FIELD_FLAGS = 2, LBM_FIELD_F = 3, LBM_FIELD_FI = 4 };
 enum { LBM_TYPE_S = 0x01, LBM_TYPE_E = 0x02, LBM_TYPE_T = 0x04, LBM_TYPE_F = 0x08,
        LBM_TYPE_I = 0x10, LBM_TYPE_G = 0x20, LBM_TYPE_X = 0x40, LBM_TYPE_Y = 0x80 };
@@ -60,6 +66,7 @@ typedef struct lbm_config {
 	int32_t device;          /* CUDA device ordinal; -1: the calling thread's current device */
 	float nu;                /* kinematic shear viscosity, > 0 */
 	float fx, fy, fz;        /* global volume force (needs LBM_EXT_VOLUME_FORCE when non-zero) */
+	uint32_t arithmetic;     /* LBM_ARITH_AUTO (0), LBM_ARITH_EXACT or LBM_ARITH_FAST */
 } lbm_config;
 
 /* ---- lifetime: replaces LBM_Domain::LBM_Domain + allocate (src/lbm.cpp:96-176) and the
@@ -119,6 +126,31 @@ int lbm_voxelize_mesh(lbm_domain* domain, const float* p0, const float* p1, cons
                       const float center[3], const float linear_velocity[3], const float rotational_velocity[3]);
 /* clears `flag` in the mesh bounding box +-1 cell */
 int lbm_unvoxelize_mesh(lbm_domain* domain, const float pmin[3], const float pmax[3], uint8_t flag);
+
+/* ---- adjoint (no counterpart in the reference): gradient of an objective J with respect to the
+ *      per-cell force field F (LBM_EXT_VOLUME_FORCE and LBM_EXT_FORCE_FIELD required). The forward run
+ *      starts at the domain's current time step t0 (after lbm_initialize) and advances it by `steps`,
+ *      exactly like lbm_stream_collide; the discrete adjoint then runs backwards through the same steps,
+ *      recomputing them from DDF snapshots taken every checkpoint_interval steps. */
+enum { LBM_OBJECTIVE_KINETIC_ENERGY_PLANE_X = 1, /* mean of 1/2 rho |u|^2 over the fluid cells of plane x */
+       LBM_OBJECTIVE_DRAG_X = 2 };             /* x component of the force on cells with flags == marker */
+typedef struct lbm_adjoint_config {
+	uint64_t steps;               /* forward time steps */
+	uint64_t checkpoint_interval; /* DDF snapshot every this many steps (>= 1) */
+	uint32_t objective;           /* LBM_OBJECTIVE_* */
+	uint32_t plane_x;             /* KINETIC_ENERGY_PLANE_X: plane */
+	uint32_t marker;              /* DRAG_X: flag value of the object's cells */
+	uint32_t reserved;
+	uint64_t window_begin, window_end; /* J is the mean over the states after these time steps (inclusive) */
+} lbm_adjoint_config;
+typedef struct lbm_adjoint_stats {
+	double forward_ms, recompute_ms, adjoint_ms; /* device time of the three phases */
+	uint64_t workspace_bytes;                    /* snapshots + recomputed states + adjoint DDFs + gradient */
+	uint32_t levels;                             /* 1: every state of a segment kept; 2: sub-snapshots inside segments */
+	uint32_t reserved;
+} lbm_adjoint_stats;
+/* J (objective, may be NULL), dJ/dF (gradient: host float[3N] SoA, may be NULL), stats (may be NULL) */
+int lbm_run_adjoint(lbm_domain* domain, const lbm_adjoint_config* config, double* objective, float* gradient, lbm_adjoint_stats* stats);
 
 /* ---- page-locked host buffers for fast field transfers (the reference's Memory<T> host side,
  *      src/opencl.hpp:342-440, is plain pageable memory) */

@@ -219,3 +219,46 @@ class RefHarness:
     def unvoxelize_mesh(self, flag, x0, y0, z0, x1, y1, z1):
         self._cfg()
         self.L.ref_unvoxelize_mesh(_p(self.flags), flag, x0, y0, z0, x1, y1, z1)
+
+
+class OracleObjective(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_uint32), ("plane_x", ctypes.c_uint32), ("marker", ctypes.c_uint32), ("pad", ctypes.c_uint32),
+                ("t_begin", ctypes.c_uint64), ("t_end", ctypes.c_uint64)]
+
+
+OBJ_KE_PLANE, OBJ_DRAG_X = 1, 2
+
+
+def objective(kind, t_begin, t_end, plane_x=0, marker=0):
+    k = {"ke_plane": OBJ_KE_PLANE, "drag_x": OBJ_DRAG_X}[kind]
+    return OracleObjective(k, plane_x, marker, 0, t_begin, t_end)
+
+
+def _adjoint_lib():
+    L = lib()
+    if not getattr(L, "_adjoint_typed", False):
+        v, d, u64 = ctypes.c_void_p, ctypes.c_double, ctypes.c_uint64
+        cfg, obj = ctypes.POINTER(OracleConfig), ctypes.POINTER(OracleObjective)
+        L.oracle_objective_f64.argtypes = [cfg, v, v, v, v, v, d, d, d, u64, obj]
+        L.oracle_objective_f64.restype = d
+        L.oracle_adjoint_f64.argtypes = [cfg, v, v, v, v, v, d, d, d, u64, obj, u64, ctypes.POINTER(d), v]
+        L._adjoint_typed = True
+    return L
+
+
+def fp64_objective(o: "Oracle", f0, steps, obj, force=(0.0, 0.0, 0.0), F=None):
+    """J of a forward FP64 run of `steps` steps from the initialised DDFs f0 (o must be precision f64)."""
+    F = o.F if F is None else np.ascontiguousarray(F, np.float64)
+    return float(_adjoint_lib().oracle_objective_f64(ctypes.byref(o.cfg), _p(f0), _p(o.flags), _p(o.rho), _p(o.u), _p(F), *force, steps,
+                                                     ctypes.byref(obj)))
+
+
+def fp64_adjoint(o: "Oracle", f0, steps, obj, interval, force=(0.0, 0.0, 0.0)):
+    """(J, dJ/dF) by the checkpointed FP64 discrete adjoint."""
+    grad = np.zeros(3 * o.N, np.float64)
+    J = ctypes.c_double()
+    rc = _adjoint_lib().oracle_adjoint_f64(ctypes.byref(o.cfg), _p(f0), _p(o.flags), _p(o.rho), _p(o.u), _p(o.F), *force, steps,
+                                           ctypes.byref(obj), interval, ctypes.byref(J), _p(grad))
+    if rc != 0:
+        raise RuntimeError("oracle adjoint failed")
+    return J.value, grad

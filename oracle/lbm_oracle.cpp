@@ -538,3 +538,261 @@ u16 oracle_fp16c_encode(const float x) { return float_to_fp16c(x); }
 float oracle_fp16c_decode(const u16 h) { return fp16c_to_float(h); }
 
 } // extern "C"
+
+// ==================================================================== adjoint (FP64), no reference
+// Discrete adjoint of the forward step above, for dJ/dF with F the per-cell FORCE_FIELD force.
+// A step maps the slots of each fluid cell n (its Esoteric-Pull slot set at the step's parity) to
+// themselves: gather g (load_f), h = Phi(g; F_n), scatter h (store_f). The adjoint of step k is
+// therefore local and in place: with lambda^{k+1} read at the store positions (hbar), the cell
+// computes gbar = (dPhi/dg)^T hbar + dj_k/dg and writes it at the load positions; solid cells map
+// their slots identically; F_bar accumulates (dPhi/dF)^T hbar. Objectives (averaged over a window
+// of time steps k, each term a function of the state after k steps):
+//   OBJ_KE_PLANE: mean over fluid cells of plane x=X of 1/2 rho |u|^2, rho/u as update_fields gives;
+//   OBJ_DRAG_X:   sum over cells with flags==marker of F_x from update_force_field (= 2 m_x).
+extern "C" struct OracleObjective {
+	u32 kind;        // 1: OBJ_KE_PLANE, 2: OBJ_DRAG_X
+	u32 plane_x;     // OBJ_KE_PLANE
+	u32 marker;      // OBJ_DRAG_X
+	u32 pad;
+	u64 t_begin, t_end; // window [t_begin, t_end] of time steps (inclusive)
+};
+enum { OBJ_KE_PLANE = 1, OBJ_DRAG_X = 2 };
+
+struct CellFwd { // forward quantities of one fluid cell needed by its adjoint
+	double rho, m[3], u0[3], v[3], u[3], Ft[3], rho2, c3;
+	bool kappa[3];
+};
+
+static void cell_forward_f64(const OracleConfig* c, const double* g, const bool is_e, const double rho_p, const double* u_p, const double* Ft, CellFwd& s) {
+	const u32 q = c->q;
+	const bool vf = (c->ext&EXT_VOLUME_FORCE)!=0u;
+	const double cs = sound_speed<double>();
+	if(is_e) { s.rho = rho_p; for(int d=0; d<3; d++) { s.u0[d] = u_p[d]; s.m[d] = 0.0; } }
+	else {
+		double rho = 0.0; for(u32 i=0u; i<q; i++) rho += g[i]; rho += 1.0;
+		s.rho = rho;
+		for(int d=0; d<3; d++) { double m = 0.0; for(u32 i=1u; i<q; i++) m += cq(q, d, i)*g[i]; s.m[d] = m; s.u0[d] = m/rho; }
+	}
+	s.rho2 = 0.5/s.rho;
+	for(int d=0; d<3; d++) {
+		s.Ft[d] = Ft[d];
+		s.v[d] = vf ? s.u0[d]+Ft[d]*s.rho2 : s.u0[d];
+		s.kappa[d] = s.v[d]>-cs && s.v[d]<cs;
+		s.u[d] = std::fmin(std::fmax(s.v[d], -cs), cs);
+	}
+	s.c3 = -3.0*(s.u[0]*s.u[0]+s.u[1]*s.u[1]+s.u[2]*s.u[2]);
+}
+
+// gbar = (dh/dg)^T hbar (+ objective ke_weight * d(1/2 rho |u|^2)/dg) and Fbar += (dh/dF_total)^T hbar
+static void cell_adjoint_f64(const OracleConfig* c, const CellFwd& s, const bool is_e, const double* hbar, const double ke_weight, double* gbar, double* Fbar) {
+	const u32 q = c->q;
+	const bool vf = (c->ext&EXT_VOLUME_FORCE)!=0u;
+	const Weights<double> W = weights<double>(q);
+	const double w = c->w;
+	const double wm = 1.0/(0.1875/(1.0/w-0.5)+0.5);
+	const double hp = 0.5*w, hm = 0.5*wm, c_tau = 1.0-0.5*w, c_taup = 0.5-0.25*w, c_taum = 0.5-0.25*wm;
+	double feqbar[27], Gbar[27];
+	for(u32 i=0u; i<q; i++) { gbar[i] = 0.0; feqbar[i] = 0.0; Gbar[i] = 0.0; }
+	if(is_e) {
+		for(u32 i=0u; i<q; i++) feqbar[i] = hbar[i];
+	} else if(!c->trt) {
+		for(u32 i=0u; i<q; i++) { gbar[i] = (1.0-w)*hbar[i]; feqbar[i] = w*hbar[i]; Gbar[i] = c_tau*hbar[i]; }
+	} else {
+		gbar[0] = (1.0-2.0*hp)*hbar[0]; feqbar[0] = 2.0*hp*hbar[0]; Gbar[0] = 2.0*c_taup*hbar[0];
+		for(u32 i=1u; i<q; i+=2u) {
+			const double a = hbar[i], b = hbar[i+1u];
+			const double di = hp*(a+b)+hm*(a-b), dj = hp*(a+b)-hm*(a-b);
+			gbar[i] = a-di; gbar[i+1u] = b-dj; feqbar[i] = di; feqbar[i+1u] = dj;
+			Gbar[i] = c_taup*(a+b)+c_taum*(a-b); Gbar[i+1u] = c_taup*(a+b)-c_taum*(a-b);
+		}
+	}
+	// equilibrium: feq_i = w_i (rho (0.5 (uk^2 + c3) + uk) + rho - 1), uk = 3 c_i.u, c3 = -3 |u|^2
+	double rhobar = 0.0, ubar[3] = {0.0, 0.0, 0.0};
+	for(u32 i=0u; i<q; i++) {
+		const double wi = weight(W, i);
+		double uk = 0.0; for(int d=0; d<3; d++) uk += 3.0*cq(q, d, i)*s.u[d];
+		rhobar += feqbar[i]*wi*(0.5*(uk*uk+s.c3)+uk+1.0);
+		for(int d=0; d<3; d++) ubar[d] += feqbar[i]*wi*s.rho*(3.0*cq(q, d, i)*(uk+1.0)-3.0*s.u[d]);
+	}
+	// Guo forcing: G_i = 9 w_i (cf (cu + 1/3) + uF), cf = c_i.Ft, cu = c_i.u, uF = -u.Ft/3
+	double Ftbar[3] = {0.0, 0.0, 0.0};
+	if(vf && !is_e) {
+		for(u32 i=0u; i<q; i++) {
+			const double wi9 = 9.0*weight(W, i);
+			double cf = 0.0, cu = 0.0; for(int d=0; d<3; d++) { cf += cq(q, d, i)*s.Ft[d]; cu += cq(q, d, i)*s.u[d]; }
+			for(int d=0; d<3; d++) {
+				ubar[d] += Gbar[i]*wi9*(cf*cq(q, d, i)-s.Ft[d]/3.0);
+				Ftbar[d] += Gbar[i]*wi9*(cq(q, d, i)*(cu+1.0/3.0)-s.u[d]/3.0);
+			}
+		}
+	}
+	if(ke_weight!=0.0 && !is_e) { // objective term 1/2 rho |u|^2 of this cell
+		rhobar += ke_weight*0.5*(s.u[0]*s.u[0]+s.u[1]*s.u[1]+s.u[2]*s.u[2]);
+		for(int d=0; d<3; d++) ubar[d] += ke_weight*s.rho*s.u[d];
+	}
+	// clamp, force shift u = u0 + Ft*0.5/rho, u0 = m/rho
+	double u0bar[3], rho2bar = 0.0;
+	for(int d=0; d<3; d++) {
+		const double vbar = s.kappa[d] ? ubar[d] : 0.0;
+		u0bar[d] = vbar;
+		if(vf) { Ftbar[d] += vbar*s.rho2; rho2bar += vbar*s.Ft[d]; }
+	}
+	if(!is_e) {
+		rhobar += rho2bar*(-0.5/(s.rho*s.rho));
+		double mbar[3];
+		for(int d=0; d<3; d++) { mbar[d] = u0bar[d]/s.rho; rhobar -= u0bar[d]*s.u0[d]/s.rho; }
+		for(u32 i=0u; i<q; i++) {
+			gbar[i] += rhobar;
+			for(int d=0; d<3; d++) gbar[i] += cq(q, d, i)*mbar[d];
+		}
+	}
+	for(int d=0; d<3; d++) Fbar[d] += Ftbar[d];
+}
+
+// objective of the state at time step t (f in FP64 storage), and its gradient added to lambda when lambda != nullptr
+static double objective_state_f64(const OracleConfig* c, const OracleObjective* obj, const double* f, const u8* flags, const double* rho_p, const double* u_p,
+                                  const double* F, const double fx, const double fy, const double fz, const u64 t, const double weight, double* lambda,
+                                  double* grad) {
+	const Grid G(c); const u32 q = c->q;
+	const bool ff = (c->ext&EXT_FORCE_FIELD)!=0u, eq = (c->ext&EXT_EQUILIBRIUM_BOUNDARIES)!=0u;
+	double J = 0.0;
+	for(u64 n=0ull; n<G.N; n++) {
+		const u8 fl = flags[n];
+		u32 x, y, z; G.coords(n, x, y, z);
+		const bool solid = (fl&T_BO)==T_S;
+		if(obj->kind==OBJ_KE_PLANE) {
+			if(x!=obj->plane_x || solid || (fl&T_SU)==T_G || (eq && (fl&T_BO)==T_E)) continue;
+		} else {
+			if(fl!=(u8)obj->marker) continue;
+		}
+		u64 j[27]; G.neighbors(n, q, j);
+		double g[27]; load_f<double>(n, g, f, j, t, q, G.N, ST_FP32);
+		double slot_grad[27];
+		if(obj->kind==OBJ_KE_PLANE) {
+			CellFwd s;
+			const double Ft[3] = {fx+(ff ? F[n] : 0.0), fy+(ff ? F[G.N+n] : 0.0), fz+(ff ? F[2ull*G.N+n] : 0.0)};
+			const double up[3] = {u_p[n], u_p[G.N+n], u_p[2ull*G.N+n]};
+			cell_forward_f64(c, g, false, rho_p[n], up, Ft, s);
+			J += weight*0.5*s.rho*(s.u[0]*s.u[0]+s.u[1]*s.u[1]+s.u[2]*s.u[2]);
+			if(!lambda) continue;
+			double zero[27] = {0.0}, Fb[3] = {0.0, 0.0, 0.0};
+			cell_adjoint_f64(c, s, false, zero, weight, slot_grad, Fb);
+			if(ff && grad) { grad[n] += Fb[0]; grad[G.N+n] += Fb[1]; grad[2ull*G.N+n] += Fb[2]; } // the velocity includes F/(2 rho)
+		} else {
+			double m = 0.0; for(u32 i=1u; i<q; i++) m += cq(q, 0, i)*g[i];
+			J += weight*2.0*m;
+			if(!lambda) continue;
+			for(u32 i=0u; i<q; i++) slot_grad[i] = weight*2.0*cq(q, 0, i);
+		}
+		// add at the load positions of parity t
+		lambda[n] += slot_grad[0];
+		for(u32 i=1u; i<q; i+=2u) {
+			lambda[(u64)(t%2ull ? i : i+1u)*G.N+n] += slot_grad[i];
+			lambda[(u64)(t%2ull ? i+1u : i)*G.N+j[i]] += slot_grad[i+1u];
+		}
+	}
+	return J;
+}
+
+static double obj_weight(const OracleObjective* obj, const Grid& G, const u8* flags, const OracleConfig* c, const u64 t) {
+	if(t<obj->t_begin||t>obj->t_end) return 0.0;
+	const double steps = (double)(obj->t_end-obj->t_begin+1ull);
+	if(obj->kind==OBJ_DRAG_X) return 1.0/steps;
+	u64 cells = 0ull; // fluid cells of the plane
+	const bool eq = (c->ext&EXT_EQUILIBRIUM_BOUNDARIES)!=0u;
+	for(u64 n=0ull; n<G.N; n++) {
+		u32 x, y, z; G.coords(n, x, y, z);
+		const u8 fl = flags[n];
+		if(x==obj->plane_x && (fl&T_BO)!=T_S && (fl&T_SU)!=T_G && !(eq && (fl&T_BO)==T_E)) cells++;
+	}
+	return cells ? 1.0/(steps*(double)cells) : 0.0;
+}
+
+// lambda^k = A_k^T lambda^{k+1} in place (fluid cells; solid and gas cells map their slots identically),
+// grad += (dPhi_k/dF)^T lambda^{k+1}
+static void adjoint_step_f64(const OracleConfig* c, const double* f, double* lambda, const u8* flags, const double* rho_p, const double* u_p,
+                             const double* F, const double fx, const double fy, const double fz, const u64 t, double* grad) {
+	const Grid G(c); const u32 q = c->q;
+	const bool ff = (c->ext&EXT_FORCE_FIELD)!=0u, eq = (c->ext&EXT_EQUILIBRIUM_BOUNDARIES)!=0u;
+	parallel_cells(G.N, c->threads, [&](const u64 n) {
+		const u8 fl = flags[n];
+		if((fl&T_BO)==T_S||(fl&T_SU)==T_G) return;
+		u64 j[27]; G.neighbors(n, q, j);
+		double g[27], hbar[27], gbar[27];
+		load_f<double>(n, g, f, j, t, q, G.N, ST_FP32);
+		u64 A[27], B[27];
+		hbar[0] = lambda[n];
+		for(u32 i=1u; i<q; i+=2u) {
+			A[i] = (u64)(t%2ull ? i : i+1u)*G.N+n; B[i] = (u64)(t%2ull ? i+1u : i)*G.N+j[i];
+			hbar[i] = lambda[B[i]]; hbar[i+1u] = lambda[A[i]];
+		}
+		const bool is_e = eq && (fl&T_BO)==T_E;
+		const double Ft[3] = {fx+(ff ? F[n] : 0.0), fy+(ff ? F[G.N+n] : 0.0), fz+(ff ? F[2ull*G.N+n] : 0.0)};
+		const double up[3] = {u_p[n], u_p[G.N+n], u_p[2ull*G.N+n]};
+		CellFwd s;
+		cell_forward_f64(c, g, is_e, rho_p[n], up, Ft, s);
+		double Fb[3] = {0.0, 0.0, 0.0};
+		cell_adjoint_f64(c, s, is_e, hbar, 0.0, gbar, Fb);
+		lambda[n] = gbar[0];
+		for(u32 i=1u; i<q; i+=2u) { lambda[A[i]] = gbar[i]; lambda[B[i]] = gbar[i+1u]; }
+		if(ff && grad) { grad[n] += Fb[0]; grad[G.N+n] += Fb[1]; grad[2ull*G.N+n] += Fb[2]; }
+	});
+}
+
+extern "C" {
+
+// J of a forward run of `steps` steps from the initialised state f0 (copied, not modified)
+double oracle_objective_f64(const OracleConfig* c, const double* f0, const u8* flags, const double* rho_p, const double* u_p, const double* F,
+                            const double fx, const double fy, const double fz, const u64 steps, const OracleObjective* obj) {
+	const Grid G(c);
+	std::vector<double> f(f0, f0+(size_t)c->q*G.N);
+	double J = 0.0;
+	for(u64 t=0ull; t<=steps; t++) {
+		const double wgt = obj_weight(obj, G, flags, c, t);
+		if(wgt!=0.0) J += objective_state_f64(c, obj, f.data(), flags, rho_p, u_p, F, fx, fy, fz, t, wgt, nullptr, nullptr);
+		if(t<steps) stream_collide_t<double>(c, f.data(), rho_p, u_p, flags, t, fx, fy, fz, F);
+	}
+	return J;
+}
+
+// J and dJ/dF (grad, 3N, overwritten) by the checkpointed discrete adjoint: snapshots every
+// `interval` steps in the forward sweep, each segment recomputed from its snapshot in the reverse sweep
+int oracle_adjoint_f64(const OracleConfig* c, const double* f0, const u8* flags, const double* rho_p, const double* u_p, const double* F,
+                       const double fx, const double fy, const double fz, const u64 steps, const OracleObjective* obj, const u64 interval,
+                       double* J_out, double* grad) {
+	if(!valid(c)||interval==0ull) return -1;
+	const Grid G(c);
+	const size_t S = (size_t)c->q*G.N;
+	std::vector<std::vector<double>> snaps;
+	std::vector<double> f(f0, f0+S);
+	double J = 0.0;
+	for(u64 t=0ull; t<=steps; t++) {
+		if(t%interval==0ull && t<steps) snaps.push_back(f);
+		const double wgt = obj_weight(obj, G, flags, c, t);
+		if(wgt!=0.0) J += objective_state_f64(c, obj, f.data(), flags, rho_p, u_p, F, fx, fy, fz, t, wgt, nullptr, nullptr);
+		if(t<steps) stream_collide_t<double>(c, f.data(), rho_p, u_p, flags, t, fx, fy, fz, F);
+	}
+	std::vector<double> lambda(S, 0.0);
+	for(size_t i=0u; i<3u*G.N; i++) grad[i] = 0.0;
+	{ const double wgt = obj_weight(obj, G, flags, c, steps); if(wgt!=0.0) objective_state_f64(c, obj, f.data(), flags, rho_p, u_p, F, fx, fy, fz, steps, wgt, lambda.data(), grad); }
+	std::vector<std::vector<double>> seg;
+	for(u64 s=snaps.size(); s-->0ull;) {
+		const u64 k0 = s*interval, k1 = std::min<u64>(k0+interval, steps);
+		seg.assign((size_t)(k1-k0), std::vector<double>());
+		std::vector<double> w = snaps[(size_t)s];
+		for(u64 k=k0; k<k1; k++) {
+			seg[(size_t)(k-k0)] = w;
+			if(k+1ull<k1) stream_collide_t<double>(c, w.data(), rho_p, u_p, flags, k, fx, fy, fz, F);
+		}
+		for(u64 k=k1; k-->k0;) {
+			const std::vector<double>& fk = seg[(size_t)(k-k0)];
+			adjoint_step_f64(c, fk.data(), lambda.data(), flags, rho_p, u_p, F, fx, fy, fz, k, grad);
+			const double wgt = obj_weight(obj, G, flags, c, k);
+			if(wgt!=0.0) objective_state_f64(c, obj, fk.data(), flags, rho_p, u_p, F, fx, fy, fz, k, wgt, lambda.data(), grad);
+		}
+	}
+	*J_out = J;
+	return 0;
+}
+
+} // extern "C"

@@ -2,6 +2,7 @@
 // "binary identity" probe at :58), compiled against fluidx3d_gb300/host/lbm.hpp: 64^3 Taylor-Green
 // vortex, D3Q19 SRT FP32, nu = 1/30, 1000 steps. Writes rho and u (raw float32) to argv[1] and
 // prints u.x at the box centre.
+#define EXACT_ARITHMETIC // bit-identical to the reference
 #include "lbm.hpp"
 
 int main(int argc, char** argv) {

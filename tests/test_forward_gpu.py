@@ -17,9 +17,9 @@ def sha(a):
     return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
 
 
-def make_gpu(case):
+def make_gpu(case, arithmetic="exact"):
     lbm = LBM(*case.shape, case.nu, *case.force, velocity_set=case.q, collision=case.collision, storage=case.storage,
-              extensions=case.extensions)
+              extensions=case.extensions, arithmetic=arithmetic)
     f = case.fields()
     lbm.rho.data[:], lbm.u.data[:], lbm.flags.data[:], lbm.F.data[:] = f["rho"], f["u"], f["flags"], f["F"]
     return lbm
@@ -140,7 +140,7 @@ def test_odd_lattices_random_flags(storage, shape, gpu):
     ext = ("eq", "ff", "vf")
     o = oracle.Oracle(Nx, Ny, Nz, q=19, collision="trt", storage=storage, extensions=ext, nu=0.02)
     o.rho[:], o.u[:], o.flags[:], o.F[:] = f["rho"], f["u"], f["flags"], f["F"]
-    with LBM(Nx, Ny, Nz, 0.02, 3e-5, -1e-5, 2e-5, collision="trt", storage=storage, extensions=ext) as lbm:
+    with LBM(Nx, Ny, Nz, 0.02, 3e-5, -1e-5, 2e-5, collision="trt", storage=storage, extensions=ext, arithmetic="exact") as lbm:
         lbm.rho.data[:], lbm.u.data[:], lbm.flags.data[:], lbm.F.data[:] = f["rho"], f["u"], f["flags"], f["F"]
         o.initialize()
         lbm.run(5)
