@@ -123,6 +123,12 @@ struct RowStageLayout {
 	}
 };
 
+// lattice velocities as a table the bulk-copy lanes index at run time
+__constant__ int8_t c_vs_tab[3][27] = {
+	{0, 1,-1, 0, 0, 0, 0, 1,-1, 1,-1, 0, 0, 1,-1, 1,-1, 0, 0, 1,-1, 1,-1, 1,-1,-1, 1},
+	{0, 0, 0, 1,-1, 0, 0, 1,-1, 0, 0, 1,-1,-1, 1, 0, 0, 1,-1, 1,-1, 1,-1,-1, 1, 1,-1},
+	{0, 0, 0, 0, 0, 1,-1, 0, 0, 1,-1, 1,-1, 0, 0,-1, 1,-1, 1, 1,-1,-1, 1, 1,-1, 1,-1}};
+
 template<int Q, int ST, bool TRT, int EXT, bool FAST> __global__ void __launch_bounds__(ROW_TPB_MAX, (Q==19 ? 2 : 1))
 k_stream_collide_rows(const StepArgs a, const uint32_t stages) {
 	typedef typename Codec<ST>::T T;
@@ -140,43 +146,47 @@ k_stream_collide_rows(const StepArgs a, const uint32_t stages) {
 	const T* src = (const T*)a.fi;
 	T* dst = (T*)a.fi_dst;
 	const uint32_t P = stages>2u ? stages-2u : 1u; // x-rows loaded ahead of the one being collided
-	// global start of DDF slot row s of x-row (y,z): 0; i (odd): own slot; i+1: neighbour slot
-	auto grow = [&](auto ic, const uint32_t y, const uint32_t z) -> uint64_t {
-		constexpr int s = decltype(ic)::value;
-		const uint64_t row0 = ((uint64_t)z*Ny+y)*Nx;
-		if constexpr(s==0) return row0;
-		else if constexpr(s%2==1) return (uint64_t)(odd ? s : s+1)*N+row0;
-		else {
-			constexpr int i = s-1, cy = vs_c(1, i), cz = vs_c(2, i);
-			const uint32_t yy = cy>0 ? (y+1u==Ny ? 0u : y+1u) : cy<0 ? (y==0u ? Ny-1u : y-1u) : y;
-			const uint32_t zz = cz>0 ? (z+1u==Nz ? 0u : z+1u) : cz<0 ? (z==0u ? Nz-1u : z-1u) : z;
-			return (uint64_t)(odd ? i+1 : i)*N+((uint64_t)zz*Ny+yy)*Nx;
-		}
+	// bulk-copy lanes: lane k<Q of warp 0 moves DDF slot row k of every x-row, lane Q its flags row.
+	// Slot row k of x-row (y,z) is row (y+dy, z+dz) of array karr: slot 0 and odd slots (own slots)
+	// sit in the x-row itself, slot i+1 (i odd) in the neighbour row along c_i.
+	const bool copier = tid<=(uint32_t)Q;
+	uint32_t karr = 0u; int dy = 0, dz = 0;
+	if(copier && tid<(uint32_t)Q && tid>0u) {
+		const uint32_t k = tid;
+		if(k%2u==1u) karr = odd ? k : k+1u;
+		else { karr = odd ? k : k-1u; dy = c_vs_tab[1][k-1u]; dz = c_vs_tab[2][k-1u]; }
+	}
+	auto row_of = [&](const uint64_t r, uint32_t& y, uint32_t& z) { z = (uint32_t)(r/Ny); y = (uint32_t)(r-(uint64_t)z*Ny); };
+	auto slot_row = [&](const uint32_t y, const uint32_t z) -> uint64_t { // global start of this lane's slot row
+		const uint32_t yy = dy>0 ? (y+1u==Ny ? 0u : y+1u) : dy<0 ? (y==0u ? Ny-1u : y-1u) : y;
+		const uint32_t zz = dz>0 ? (z+1u==Nz ? 0u : z+1u) : dz<0 ? (z==0u ? Nz-1u : z-1u) : z;
+		return (uint64_t)karr*N+((uint64_t)zz*Ny+yy)*Nx;
 	};
-	auto issue_loads = [&](const uint32_t r, const uint32_t s) { // thread 0 only
-		const uint32_t z = r/Ny, y = r-z*Ny;
+	auto issue_loads = [&](const uint64_t r, const uint32_t s) { // all lanes of warp 0
+		uint32_t y, z; row_of(r, y, z);
 		unsigned char* st = stage0+(size_t)s*L.stage_bytes;
-		uint64_t* bar = bars+s;
-		mbar_arrive_expect_tx(bar, (uint32_t)Q*L.rowbytes+Nx);
-		Unroll<0, Q, 1>::run([&](auto ic) { bulk_load(st+(size_t)decltype(ic)::value*L.stride, src+grow(ic, y, z), L.rowbytes, bar); });
-		bulk_load(st+L.flags_off, a.flags+((uint64_t)z*Ny+y)*Nx, Nx, bar);
+		if(tid==0u) mbar_arrive_expect_tx(bars+s, (uint32_t)Q*L.rowbytes+Nx);
+		__syncwarp();
+		if(tid<(uint32_t)Q) bulk_load(st+(size_t)tid*L.stride, src+slot_row(y, z), L.rowbytes, bars+s);
+		else if(tid==(uint32_t)Q) bulk_load(st+L.flags_off, a.flags+((uint64_t)z*Ny+y)*Nx, Nx, bars+s);
 	};
 	if(tid==0u) {
 		for(uint32_t s=0u; s<stages; s++) mbar_init(bars+s, 1u);
 		fence_mbar_init();
 		abort_rows = 0;
-		for(uint32_t p=0u; p<P; p++) { const uint64_t r = (uint64_t)blockIdx.x+(uint64_t)p*gridDim.x; if(r<rows) issue_loads((uint32_t)r, p); }
 	}
+	__syncwarp();
+	if(tid<32u) for(uint32_t p=0u; p<P; p++) { const uint64_t r = (uint64_t)blockIdx.x+(uint64_t)p*gridDim.x; if(r<rows) issue_loads(r, p); }
 	__syncthreads();
 	uint32_t j = 0u;
 	for(uint64_t r=blockIdx.x; r<rows; r+=gridDim.x, j++) {
 		const uint32_t s = j%stages;
-		if(tid==0u) {
+		if(tid<32u) {
 			const uint64_t rn = r+(uint64_t)P*gridDim.x;
 			if(rn<rows) {
-				// the stage of x-row j+P last held x-row j+P-stages: its stores must have left shared memory
-				if(stages-P-1u>=1u) bulk_wait_read_but1(); else bulk_wait_read_all();
-				issue_loads((uint32_t)rn, (j+P)%stages);
+				// the stage of x-row j+P last held x-row j+P-stages: this lane's store of it must have left shared memory
+				if(copier) { if(stages-P-1u>=1u) bulk_wait_read_but1(); else bulk_wait_read_all(); }
+				issue_loads(rn, (j+P)%stages);
 			}
 		}
 		const bool ok = mbar_wait_bounded(bars+s, (j/stages)&1u, a.err);
@@ -184,7 +194,7 @@ k_stream_collide_rows(const StepArgs a, const uint32_t stages) {
 		unsigned char* st = stage0+(size_t)s*L.stage_bytes;
 		auto srow = [&](const int k) { return reinterpret_cast<T*>(st+(size_t)k*L.stride); };
 		const uint8_t* fl = st+L.flags_off;
-		const uint32_t z = (uint32_t)(r/Ny), y = (uint32_t)(r-(uint64_t)z*Ny);
+		uint32_t y, z; row_of(r, y, z);
 		const uint64_t row0 = ((uint64_t)z*Ny+y)*Nx;
 		for(uint32_t x=tid; ok && x<Nx; x+=blockDim.x) {
 			const uint8_t flagsn = fl[x];
@@ -217,16 +227,16 @@ k_stream_collide_rows(const StepArgs a, const uint32_t stages) {
 					const uint64_t rp = r+(uint64_t)p*gridDim.x;
 					if(rp<rows) mbar_wait_bounded(bars+(j+p)%stages, ((j+p)/stages)&1u, nullptr);
 				}
-				bulk_wait_all();
 			}
+			if(copier) bulk_wait_all();
 			return;
 		}
-		if(tid==0u) {
-			Unroll<0, Q, 1>::run([&](auto ic) { bulk_store(dst+grow(ic, y, z), st+(size_t)decltype(ic)::value*L.stride, L.rowbytes); });
+		if(tid<(uint32_t)Q) {
+			bulk_store(dst+slot_row(y, z), st+(size_t)tid*L.stride, L.rowbytes);
 			bulk_commit();
 		}
 	}
-	if(tid==0u) bulk_wait_all(); // stores complete before the CTA (and its shared memory) goes away
+	if(copier) bulk_wait_all(); // stores complete before the CTA (and its shared memory) goes away
 }
 
 template<int Q, int ST, int EXT, bool FAST> __global__ void __launch_bounds__(BLOCK) k_update_fields(const StepArgs a) {

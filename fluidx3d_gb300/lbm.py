@@ -94,7 +94,14 @@ class LBM:
         self.rho = Field(self, C.FIELD_RHO, 1, np.float32, 1.0)
         self.u = Field(self, C.FIELD_U, 3, np.float32, 0.0)
         self.flags = Field(self, C.FIELD_FLAGS, 1, np.uint8, 0)
-        self.F = Field(self, C.FIELD_F, 3, np.float32, 0.0)
+        self._F = None
+
+    @property
+    def F(self):
+        """Host buffer of the force field (allocated on first use: 12 bytes per cell)."""
+        if self._F is None:
+            self._F = Field(self, C.FIELD_F, 3, np.float32, 0.0)
+        return self._F
 
     # ------------------------------------------------------------------ lifetime
     def close(self):
