@@ -51,6 +51,7 @@ class AdjointStats(ctypes.Structure):
 
 
 OBJECTIVES = {"ke_plane": 1, "drag_x": 2}
+OBJECT_SUM_STATIC_MAX_BLOCKS = 1216  # LBM_OBJECT_SUM_STATIC_MAX_BLOCKS
 
 # every symbol include/lbm_capi.h declares, with (argtypes, restype)
 _v, _i, _u8, _u32, _u64, _f, _d, _sz = (ctypes.c_void_p, ctypes.c_int, ctypes.c_uint8, ctypes.c_uint32, ctypes.c_uint64,
@@ -80,6 +81,7 @@ SIGNATURES = {
     "lbm_object_center_of_mass": ([_v, _u8, ctypes.POINTER(_d)], _i),
     "lbm_object_force": ([_v, _u8, ctypes.POINTER(_d)], _i),
     "lbm_object_torque": ([_v, _u8, _d, _d, _d, ctypes.POINTER(_d)], _i),
+    "lbm_object_sum_static": ([_i, _u32, _u32, _u32, _v, _v, _u8, _i, _d, _d, _d, _u32, _v, ctypes.POINTER(_d)], _i),
     "lbm_voxelize_mesh": ([_v, _v, _v, _v, _u32, _u8, ctypes.POINTER(_f), ctypes.POINTER(_f), ctypes.POINTER(_f)], _i),
     "lbm_unvoxelize_mesh": ([_v, ctypes.POINTER(_f), ctypes.POINTER(_f), _u8], _i),
     "lbm_run_adjoint": ([_v, ctypes.POINTER(AdjointConfig), ctypes.POINTER(_d), _v, ctypes.POINTER(AdjointStats)], _i),

@@ -213,6 +213,8 @@ Rates make_rates(const float w) {
 	r.c_taum = std::fmaf(wm, -0.25f, 0.5f);
 	return r;
 }
+int capi_fail(const int code, const char* message) { return fail(code, "%s", message); }
+int capi_cuda_fail(const cudaError_t e, const char* what) { return cuda_fail(e, what); }
 } // namespace fx3d
 
 extern "C" {

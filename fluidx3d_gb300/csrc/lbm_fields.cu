@@ -112,6 +112,13 @@ cudaError_t launch_object_sum(const GridDesc& g, const float* F, const uint8_t* 
 	k_object_sum_final<<<1, RB, 0, s>>>(partials, REDUCE_BLOCKS, out);
 	return cudaGetLastError();
 }
+cudaError_t launch_object_sum_blocks(const GridDesc& g, const float* F, const uint8_t* flags, const uint8_t marker, const int kind,
+                                     const double cx, const double cy, const double cz, const int blocks, double* partials, double* out, cudaStream_t s) {
+	if(blocks<1) return cudaErrorInvalidValue;
+	k_object_sum<<<blocks, RB, 0, s>>>(g, F, flags, marker, kind, cx, cy, cz, partials);
+	k_object_sum_final<<<1, RB, 0, s>>>(partials, blocks, out);
+	return cudaGetLastError();
+}
 
 // box[6] = x0,y0,z0,x1,y1,z1 (mesh bounds); cells within +-1 lose `flag`
 __global__ void __launch_bounds__(BLOCK) k_unvoxelize(const GridDesc g, uint8_t* __restrict__ flags, const uint8_t flag,

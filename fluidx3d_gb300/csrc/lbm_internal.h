@@ -76,6 +76,12 @@ FX3D_DECLARE_LAUNCHERS(fp16c)
 constexpr int REDUCE_BLOCKS = 608; // 4 blocks per SM on 152 SMs
 cudaError_t launch_object_sum(const GridDesc& g, const float* F, const uint8_t* flags, uint8_t marker, int kind,
                               double cx, double cy, double cz, double* partials, double* out, cudaStream_t s);
+// the same with `blocks` reduction blocks (partials[blocks*4]); blocks == REDUCE_BLOCKS gives the same sums
+cudaError_t launch_object_sum_blocks(const GridDesc& g, const float* F, const uint8_t* flags, uint8_t marker, int kind,
+                                     double cx, double cy, double cz, int blocks, double* partials, double* out, cudaStream_t s);
+// error reporting of the C-ABI (the message lbm_last_error returns), for entry points outside lbm_capi.cu
+int capi_fail(int code, const char* message);
+int capi_cuda_fail(cudaError_t e, const char* what);
 cudaError_t launch_unvoxelize(const GridDesc& g, uint8_t* flags, uint8_t flag, const float* box, cudaStream_t s);
 
 // voxelization (lbm_voxelize.cu); bbu: 16 floats in the reference's layout (src/lbm.cpp:280-296)

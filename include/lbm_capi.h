@@ -118,6 +118,20 @@ int lbm_object_center_of_mass(lbm_domain* domain, uint8_t marker, double out[4])
 int lbm_object_force(lbm_domain* domain, uint8_t marker, double out[3]);
 int lbm_object_torque(lbm_domain* domain, uint8_t marker, double cx, double cy, double cz, double out[3]);
 
+/* Allocation-free object sums (no counterpart in the reference): the reduction of the three calls
+ * above over device arrays the caller owns (flags[N]; F[3N], x|y|z blocks as in a domain), issued on
+ * the caller's stream, with its scratch in a fixed static device array instead of an allocation.
+ * kind 0: out = mean position (box-centred) and cell count, as lbm_object_center_of_mass;
+ * kind 1: out[0..2] = sum F; kind 2: out[0..2] = sum (p - c) x F; out[3] = 0 for kinds 1 and 2.
+ * blocks: reduction blocks, 0 = 608 (the count the domain calls use, same summation order);
+ * more than LBM_OBJECT_SUM_STATIC_MAX_BLOCKS is LBM_ERR_INVALID_ARGUMENT. Returns once the result
+ * is on the host (the stream is synchronised). The first call on a device resolves the scratch's
+ * address with cudaGetSymbolAddress: make it before any stream capture on that device. The scratch
+ * is shared by all calls on a device: calls that overlap on the GPU race. */
+#define LBM_OBJECT_SUM_STATIC_MAX_BLOCKS 1216
+int lbm_object_sum_static(int device, uint32_t Nx, uint32_t Ny, uint32_t Nz, const uint8_t* flags_device, const float* F_device,
+                          uint8_t marker, int kind, double cx, double cy, double cz, uint32_t blocks, void* cuda_stream, double out[4]);
+
 /* ---- mesh voxelization (src/lbm.cpp:275-327, 1074-1093; src/kernel.cpp:2267-2363).
  * p0/p1/p2: host arrays of `triangles` vertices, xyz interleaved (float3 p0[triangles]), in lattice
  * coordinates; center / linear_velocity / rotational_velocity as in LBM::voxelize_mesh_on_device.
