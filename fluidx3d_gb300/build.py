@@ -1,9 +1,12 @@
 """Builds the sm_103a shared library of the solver core in-tree.
 
 One nvcc process per translation unit (they compile in parallel), then one link step into
-fluidx3d_gb300/_lib/libfluidx3d_gb300.so. Everything is compiled for sm_103a only. The exact
-arithmetic mode spells every rounding as an intrinsic, so it stays uncontracted while the fast mode
-lets nvcc contract multiply-adds; host code is compiled without contraction (-ffp-contract=off).
+fluidx3d_gb300/_lib/libfluidx3d_gb300.so. Everything is compiled for sm_103a only, without
+floating-point contraction (-fmad=false for device code, -ffp-contract=off for host code): every
+fused multiply-add in the kernels is written out (fmaf / packed fma), so results do not depend on
+the compiler's fusion choices. (ptxas still fuses a packed FP32x2 multiply whose only use is a
+packed add, even with -fmad=false and explicit .rn modifiers; the kernels' arithmetic is written
+without that pattern.)
 """
 from __future__ import annotations
 
@@ -22,7 +25,7 @@ LIB_NAME = "libfluidx3d_gb300.so"
 LIB_PATH = os.path.join(OUT_DIR, LIB_NAME)
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-prec-div=true", "-prec-sqrt=true", "-ftz=false",
+NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-prec-div=true", "-prec-sqrt=true", "-ftz=false", "-fmad=false",
               "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC,-ffp-contract=off,-O2", "-I", INCLUDE, "-I", CSRC]
 
 

@@ -53,4 +53,17 @@ __device__ __forceinline__ void bulk_wait_read_but1() { asm volatile("cp.async.b
 // wait until every committed bulk store is complete (writes visible)
 __device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 
+// per-thread asynchronous global -> shared copies of 4 or 8 bytes (both addresses aligned to the size);
+// a thread waits only for its own groups, so a thread that reads back only what it copied itself
+// needs no block-wide barrier
+__device__ __forceinline__ void cp_async_4(const uint32_t dst_smem, const void* src_gmem) {
+	asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" :: "r"(dst_smem), "l"(src_gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_8(const uint32_t dst_smem, const void* src_gmem) {
+	asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" :: "r"(dst_smem), "l"(src_gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+// wait until at most N of this thread's most recent groups are still in flight
+template<int N> __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" :: "n"(N) : "memory"); }
+
 } // namespace fx3d

@@ -299,18 +299,22 @@ int lbm_domain_create(const lbm_config* c, lbm_domain** out) {
 	d->g.nx_inv = c->Nx==1u ? 0ull : (~0ull)/c->Nx+1ull; // ceil(2^64/Nx)
 	d->w = lbm_relaxation_rate(c->nu);
 	d->rates = make_rates(d->w);
-	// stream_collide implementation: FX3D_STREAM_COLLIDE_PATH=cells|rows forces one (diagnostics and
-	// tests); the default picks the row-staged kernel wherever the lattice meets its constraints
+	// stream_collide implementation: FX3D_STREAM_COLLIDE_PATH=cells|rows|pairs|pipe forces one (diagnostics
+	// and tests); the default takes a two-cell packed kernel for fast arithmetic where the lattice
+	// allows it (even Nx, fewer than 2^32 cells; with per-thread prefetch for 16-bit storage), else
+	// one thread per cell
 	if(const char* p = std::getenv("FX3D_STREAM_COLLIDE_PATH")) {
 		if(!std::strcmp(p, "cells")) d->path = PATH_CELLS;
 		else if(!std::strcmp(p, "rows")) d->path = PATH_ROWS;
+		else if(!std::strcmp(p, "pairs")) d->path = PATH_PAIRS;
+		else if(!std::strcmp(p, "pipe")) d->path = PATH_PIPE;
 	}
 
 	cudaError_t e = cudaStreamCreateWithFlags(&d->own_stream, cudaStreamNonBlocking);
 	if(e==cudaSuccess) { d->stream = d->own_stream; e = cudaMalloc(&d->fi, d->field_bytes(LBM_FIELD_FI)); }
 	if(e==cudaSuccess) e = cudaMalloc(&d->rho, N*4u);
 	if(e==cudaSuccess) e = cudaMalloc(&d->u, N*12u);
-	if(e==cudaSuccess) e = cudaMalloc(&d->flags, N);
+	if(e==cudaSuccess) e = cudaMalloc(&d->flags, (N+15u)&~(uint64_t)15u); // padded: kernels read flags as aligned 4-byte words
 	if(e==cudaSuccess && (c->extensions&LBM_EXT_FORCE_FIELD)) e = cudaMalloc(&d->F, N*12u);
 	if(e==cudaSuccess) e = cudaMalloc(&d->partials, (size_t)REDUCE_BLOCKS*4u*sizeof(double));
 	if(e==cudaSuccess) e = cudaMalloc(&d->sum_dev, 4u*sizeof(double));
@@ -561,14 +565,14 @@ struct DeviceBuffer { // freed on scope exit
 int step_out_of_place(lbm_domain* d, const void* src, void* dst, const uint64_t t) {
 	StepArgs a = d->args();
 	a.t = t;
-	const bool rows = d->path!=PATH_CELLS && row_plan(d->v.q, d->v.storage, d->g.Nx, d->g.Ny, d->g.Nz).stages!=0u;
+	const bool rows = (d->path==PATH_AUTO||d->path==PATH_ROWS) && row_plan(d->v.q, d->v.storage, d->g.Nx, d->g.Ny, d->g.Nz).stages!=0u;
 	if(rows) { a.fi = const_cast<void*>(src); a.fi_dst = dst; }
 	else {
 		FX3D_CUDA(cudaMemcpyAsync(dst, src, d->field_bytes(LBM_FIELD_FI), cudaMemcpyDeviceToDevice, d->stream), "cudaMemcpyAsync(state)");
 		a.fi = dst; a.fi_dst = dst;
 	}
 	cudaError_t e;
-	const int path = rows ? PATH_ROWS : PATH_CELLS;
+	const int path = rows ? PATH_ROWS : (d->path==PATH_PAIRS||d->path==PATH_PIPE) ? d->path : PATH_CELLS;
 	switch(d->v.storage) {
 		case ST_FP32: e = launch_stream_collide_fp32(d->v, a, path, d->stream); break;
 		case ST_FP16S: e = launch_stream_collide_fp16s(d->v, a, path, d->stream); break;

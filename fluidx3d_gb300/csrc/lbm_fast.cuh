@@ -1,19 +1,28 @@
-// Fast arithmetic for one LBM cell step: the reference's scheme (src/kernel.cpp:1454-1636) with the
-// freedoms its own GPU build takes (-cl-mad-enable: multiply-adds contracted; OpenCL's default
-// non-IEEE division) plus exact algebraic regroupings, at about a third of the issued instructions
-// of the operation-for-operation form in lbm_scheme.cuh:
+// Fast arithmetic for the LBM cell step: the reference's scheme (src/kernel.cpp:1454-1636) with the
+// freedoms its own GPU build takes (-cl-mad-enable: multiply-adds fused; OpenCL's default non-IEEE
+// division) plus exact algebraic regroupings, at about a third of the issued instructions of the
+// operation-for-operation form in lbm_scheme.cuh:
 //   * DDFs stay in storage units: FP16S values are used as stored (2^15 times the DDF), so loads and
 //     stores are a bare conversion; the density carries the same factor K (R = K*rho), the Guo force
 //     terms are scaled by K and the velocity, a ratio, needs no rescaling;
-//   * one reciprocal of R per cell instead of four divisions (the velocity gets one Newton correction); rho-1 is the plain sum of the shifted
-//     DDFs (the shift is added after summing, as the reference intends with DDF shifting);
+//   * one reciprocal of R per cell instead of four divisions (the velocity gets one Newton
+//     correction); rho-1 is the plain sum of the shifted DDFs (the shift is added after summing, as
+//     the reference intends with DDF shifting);
 //   * moments from pair sums and pair differences (f_i+f_j, f_i-f_j for opposite i,j);
 //   * equilibrium of an opposite pair from one shared base term: feq_{i,j} = base +- rho w_i u_k;
 //   * TRT in symmetric / antisymmetric parts: with d = feq - f,
 //     f_i += hp (d_i+d_j) + hm (d_i-d_j) + F_i,  f_j += hp (d_i+d_j) - hm (d_i-d_j) + F_j,
 //     which equals the reference's fma(0.5wp, ..., fma(0.5wm, ..., f+Fin)) in exact arithmetic;
 //   * Guo terms of a pair from G_i+G_j = 18 w (c.F)(c.u) + 18 w uF and G_i-G_j = 6 w (c.F).
-// Results agree with the exact form to FP32 rounding (tests hold rho/u to 1e-5 relative).
+//
+// The arithmetic is written once for a value type V: float (one cell) or float2 (two cells, issued
+// as the packed FP32 instructions of sm_100 and later: add/mul.rn.f32x2, __ffma2_rn). Every
+// operation is explicitly rounded and the packed forms round each component exactly as the scalar
+// ones. ptxas fuses a packed multiply whose only use is a packed add into a packed multiply-add
+// even with explicit .rn modifiers (the scalar __fmul_rn/__fadd_rn are never fused), so no
+// multiply here feeds an add directly: each such pair is written as one fma. One cell then gives
+// bit-identical results in either form.
+// Results agree with the exact scheme to FP32 rounding (tests hold rho/u to 1e-5 relative).
 #pragma once
 #include "lbm_scheme.cuh"
 
@@ -35,7 +44,8 @@ template<> struct RawCodec<ST_FP16S> {
 // and denormal codes alike (denormal codes become FP32 denormals), so decoding is a shift and one
 // multiply by 2^112 (exact, and equal to the reference's decoder). Encoding multiplies by 2^-112 and
 // rounds the 12 dropped bits half up like the reference; for normal values that is the reference's
-// encoder bit for bit, for denormal codes it may differ in the last unit.
+// encoder bit for bit, for denormal codes it may differ in the last unit. Decoding then encoding a
+// code gives the code back.
 template<> struct RawCodec<ST_FP16C> {
 	static constexpr float K = 1.0f;
 	static __device__ __forceinline__ float decode(const uint16_t h) {
@@ -49,125 +59,202 @@ template<> struct RawCodec<ST_FP16C> {
 	}
 };
 
+// ---------------------------------------------------------------- one cell (float) or two (float2)
+__device__ __forceinline__ float v_add(const float a, const float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float v_sub(const float a, const float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float v_mul(const float a, const float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float v_fma(const float a, const float b, const float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ float v_neg(const float a) { return -a; }
+// packed add and multiply as PTX with an explicit .rn rounding modifier: the compiler never fuses
+// those into a multiply-add (as __fmul_rn/__fadd_rn), which keeps float2 results equal to float ones
+__device__ __forceinline__ float2 v_add(const float2 a, const float2 b) {
+	float2 d;
+	asm("{\n\t.reg .b64 ra, rb, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\tadd.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+	    : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+	return d;
+}
+__device__ __forceinline__ float2 v_mul(const float2 a, const float2 b) {
+	float2 d;
+	asm("{\n\t.reg .b64 ra, rb, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\tmul.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+	    : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+	return d;
+}
+__device__ __forceinline__ float2 v_neg(const float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 v_sub(const float2 a, const float2 b) { return v_add(a, v_neg(b)); } // a-b == a+(-b) in IEEE
+__device__ __forceinline__ float2 v_fma(const float2 a, const float2 b, const float2 c) { return __ffma2_rn(a, b, c); }
+template<class V> __device__ __forceinline__ V v_set(const float s);
+template<> __device__ __forceinline__ float v_set<float>(const float s) { return s; }
+template<> __device__ __forceinline__ float2 v_set<float2>(const float s) { return make_float2(s, s); }
+// a per-component function (reciprocal, clamp)
+template<class F> __device__ __forceinline__ float v_map(const float a, F&& f) { return f(a); }
+template<class F> __device__ __forceinline__ float2 v_map(const float2 a, F&& f) { return make_float2(f(a.x), f(a.y)); }
+// per-component choice: b where the lane's flag is set (flags: bool for float, Bool2 for float2)
+struct Bool2 { bool x, y; };
+__device__ __forceinline__ float v_pick(const float a, const float b, const bool s) { return s ? b : a; }
+__device__ __forceinline__ float2 v_pick(const float2 a, const float2 b, const Bool2 s) { return make_float2(s.x ? b.x : a.x, s.y ? b.y : a.y); }
+// per-cell float fields (rho, u, F) at cell n (and n+1 for float2; n even, so 8-byte aligned)
+__device__ __forceinline__ void v_load(float& v, const float* p) { v = *p; }
+__device__ __forceinline__ void v_load(float2& v, const float* p) { v = *reinterpret_cast<const float2*>(p); }
+__device__ __forceinline__ float v_clampc(const float x) { return fminf(fmaxf(x, -DEF_C), DEF_C); }
+template<class V> __device__ __forceinline__ V v_clamp(const V x) { return v_map(x, [](const float t) { return v_clampc(t); }); }
+template<class V> __device__ __forceinline__ V v_rcp(const V x) { return v_map(x, [](const float t) { return __frcp_rn(t); }); }
+
 // signed sum of v_d over the non-zero components of c_I (any order: fast mode); starts from the
-// first non-zero term, since adding to 0.0f cannot be folded away under IEEE rules
-template<int I> __device__ __forceinline__ float csum_fast(const float vx, const float vy, const float vz) {
+// first non-zero term, since adding to 0 cannot be folded away under IEEE rules
+template<int I, class V> __device__ __forceinline__ V csum_v(const V vx, const V vy, const V vz) {
 	constexpr int a = vs_c(0, I), b = vs_c(1, I), c = vs_c(2, I);
-	const float tx = a>0 ? vx : -vx, ty = b>0 ? vy : -vy, tz = c>0 ? vz : -vz;
-	if constexpr(a!=0 && b!=0 && c!=0) return tx+ty+tz;
-	else if constexpr(a!=0 && b!=0) return tx+ty;
-	else if constexpr(a!=0 && c!=0) return tx+tz;
-	else if constexpr(b!=0 && c!=0) return ty+tz;
+	const V tx = a>0 ? vx : v_neg(vx), ty = b>0 ? vy : v_neg(vy), tz = c>0 ? vz : v_neg(vz);
+	if constexpr(a!=0 && b!=0 && c!=0) return v_add(v_add(tx, ty), tz);
+	else if constexpr(a!=0 && b!=0) return v_add(tx, ty);
+	else if constexpr(a!=0 && c!=0) return v_add(tx, tz);
+	else if constexpr(b!=0 && c!=0) return v_add(ty, tz);
 	else if constexpr(a!=0) return tx;
 	else if constexpr(b!=0) return ty;
 	else return tz;
 }
 
-// accumulate d with sign c into an accumulator that starts unset (no addition to 0.0f)
-template<int C> __device__ __forceinline__ void acc_signed(float& m, bool& set, const float d) {
+// accumulate d with sign C into an accumulator that starts unset (no addition to 0)
+template<int C, class V> __device__ __forceinline__ void acc_signed(V& m, bool& set, const V d) {
 	if constexpr(C!=0) {
-		const float t = C>0 ? d : -d;
-		m = set ? m+t : t;
+		if(set) m = C>0 ? v_add(m, d) : v_sub(m, d);
+		else m = C>0 ? d : v_neg(d);
 		set = true;
 	}
 }
 
 // S = K*(rho-1) = sum of the shifted DDFs and the momentum (storage units), from pair sums and pair
 // differences; the shift K is added only afterwards (R = S+K), so S keeps full precision
-template<int Q> __device__ __forceinline__ void moments_fast(const float* f, float& S, float& mx, float& my, float& mz) {
-	float s = f[0];
+template<int Q, class V> __device__ __forceinline__ void moments_v(const V* f, V& S, V& mx, V& my, V& mz) {
+	V s = f[0];
 	bool sx = false, sy = false, sz = false;
-	mx = 0.0f; my = 0.0f; mz = 0.0f;
+	mx = v_set<V>(0.0f); my = v_set<V>(0.0f); mz = v_set<V>(0.0f);
 	Unroll<1, Q, 2>::run([&](auto ic) {
 		constexpr int i = decltype(ic)::value;
-		s += f[i]+f[i+1];
-		const float d = f[i]-f[i+1];
+		s = v_add(s, v_add(f[i], f[i+1]));
+		const V d = v_sub(f[i], f[i+1]);
 		acc_signed<vs_c(0, i)>(mx, sx, d); acc_signed<vs_c(1, i)>(my, sy, d); acc_signed<vs_c(2, i)>(mz, sz, d);
 	});
 	S = s;
 }
 
-// velocity of one cell (storage-unit DDFs or the preset TYPE_E values), force shifted and clamped;
-// returns R = K*rho, Rm1 = K*(rho-1) and 1/R
-template<int Q, int EXT, int ST> __device__ __forceinline__ void cell_rho_u_fast(const StepArgs& a, const uint64_t n, const float* f, const bool is_e,
-                                                                                float& R, float& Rm1, float& inv, float& ux, float& uy, float& uz,
-                                                                                float& fx, float& fy, float& fz) {
+// velocity of the cell(s) (storage-unit DDFs, or the preset rho/u of TYPE_E cells), force shifted and
+// clamped; R = K*rho, Rm1 = K*(rho-1), inv = 1/R. is_e: per-lane TYPE_E flags, any_e: any of them.
+template<int Q, int EXT, int ST, class V, class M> __device__ __forceinline__ void cell_rho_u_v(const StepArgs& a, const uint64_t n, const V* f, const M is_e,
+                                                                                            const bool any_e, V& R, V& Rm1, V& inv, V& ux, V& uy, V& uz,
+                                                                                            V& fx, V& fy, V& fz) {
 	constexpr bool VF = (EXT&EXT_VF)!=0, FF = (EXT&EXT_FF)!=0;
 	constexpr float K = RawCodec<ST>::K;
 	const uint64_t N = a.g.N;
-	if(is_e) {
-		R = K*a.rho[n]; Rm1 = R-K; inv = __frcp_rn(R);
-		ux = a.u[n]; uy = a.u[N+n]; uz = a.u[2ull*N+n];
-	} else {
-		float mx, my, mz;
-		moments_fast<Q>(f, Rm1, mx, my, mz);
-		R = Rm1+K;
-		inv = __frcp_rn(R);
+	auto from_fields = [&](V& R_, V& Rm1_, V& inv_, V& ux_, V& uy_, V& uz_) {
+		V r;
+		v_load(r, a.rho+n);
+		R_ = v_mul(v_set<V>(K), r); Rm1_ = v_fma(v_set<V>(K), r, v_set<V>(-K)); inv_ = v_rcp(R_);
+		v_load(ux_, a.u+n); v_load(uy_, a.u+N+n); v_load(uz_, a.u+2ull*N+n);
+	};
+	auto from_ddfs = [&]() {
+		V mx, my, mz;
+		moments_v<Q>(f, Rm1, mx, my, mz);
+		R = v_add(Rm1, v_set<V>(K));
+		inv = v_rcp(R);
 		// u = m/R from the reciprocal plus one Newton correction (u += (m - u R)/R)
-		ux = mx*inv; uy = my*inv; uz = mz*inv;
-		ux = fmaf(fmaf(-ux, R, mx), inv, ux); uy = fmaf(fmaf(-uy, R, my), inv, uy); uz = fmaf(fmaf(-uz, R, mz), inv, uz);
-	}
-	fx = a.fx; fy = a.fy; fz = a.fz;
-	if constexpr(FF) { fx += a.F[n]; fy += a.F[N+n]; fz += a.F[2ull*N+n]; }
-	if constexpr(VF) {
-		const float rho2 = (0.5f*K)*inv; // F/(2 rho) with rho = R/K
-		ux = clampc(fmaf(fx, rho2, ux)); uy = clampc(fmaf(fy, rho2, uy)); uz = clampc(fmaf(fz, rho2, uz));
+		ux = v_mul(mx, inv); uy = v_mul(my, inv); uz = v_mul(mz, inv);
+		ux = v_fma(v_fma(v_neg(ux), R, mx), inv, ux); uy = v_fma(v_fma(v_neg(uy), R, my), inv, uy); uz = v_fma(v_fma(v_neg(uz), R, mz), inv, uz);
+	};
+	if constexpr(std::is_same<V, float>::value) {
+		if(is_e) from_fields(R, Rm1, inv, ux, uy, uz);
+		else from_ddfs();
 	} else {
-		ux = clampc(ux); uy = clampc(uy); uz = clampc(uz);
+		from_ddfs();
+		if(any_e) {
+			V R2, Rm12, inv2, ux2, uy2, uz2;
+			from_fields(R2, Rm12, inv2, ux2, uy2, uz2);
+			R = v_pick(R, R2, is_e); Rm1 = v_pick(Rm1, Rm12, is_e); inv = v_pick(inv, inv2, is_e);
+			ux = v_pick(ux, ux2, is_e); uy = v_pick(uy, uy2, is_e); uz = v_pick(uz, uz2, is_e);
+		}
+	}
+	fx = v_set<V>(a.fx); fy = v_set<V>(a.fy); fz = v_set<V>(a.fz);
+	if constexpr(FF) {
+		V Fx, Fy, Fz;
+		v_load(Fx, a.F+n); v_load(Fy, a.F+N+n); v_load(Fz, a.F+2ull*N+n);
+		fx = v_add(fx, Fx); fy = v_add(fy, Fy); fz = v_add(fz, Fz);
+	}
+	if constexpr(VF) {
+		const V rho2 = v_mul(v_set<V>(0.5f*K), inv); // F/(2 rho) with rho = R/K
+		ux = v_clamp(v_fma(fx, rho2, ux)); uy = v_clamp(v_fma(fy, rho2, uy)); uz = v_clamp(v_fma(fz, rho2, uz));
+	} else {
+		ux = v_clamp(ux); uy = v_clamp(uy); uz = v_clamp(uz);
 	}
 }
 
-// collision of all directions in place, DDFs in storage units (K scaling); IS_E: TYPE_E cell (f = feq)
-template<int Q, bool TRT, bool VF, int ST, bool IS_E> __device__ __forceinline__ void collide_fast_t(float* f, const float R, const float Rm1, const float ux,
-                                                                                                 const float uy, const float uz, const float fx, const float fy,
-                                                                                                 const float fz, const StepArgs& a) {
+// collision of all directions in place, DDFs in storage units (K scaling). EMODE 0: no TYPE_E cell;
+// 1: the (single) cell is TYPE_E (f = feq); 2: mixed lanes, TYPE_E lanes picked by is_e.
+template<int Q, bool TRT, bool VF, int ST, int EMODE, class V, class M> __device__ __forceinline__ void collide_v(V* f, const V R, const V Rm1, const V ux, const V uy,
+                                                                                                             const V uz, const V fx, const V fy, const V fz,
+                                                                                                             const M is_e, const StepArgs& a) {
 	constexpr float K = RawCodec<ST>::K;
-	const float c3 = -3.0f*fmaf(ux, ux, fmaf(uy, uy, uz*uz));
-	const float ux3 = 3.0f*ux, uy3 = 3.0f*uy, uz3 = 3.0f*uz;
-	const float fxK = K*fx, fyK = K*fy, fzK = K*fz; // Guo terms in storage units
-	const float uF = VF ? -THIRD*fmaf(ux, fxK, fmaf(uy, fyK, uz*fzK)) : 0.0f;
-	{ // center
-		const float fe = vs_w<Q>(0)*fmaf(R, 0.5f*c3, Rm1);
-		if constexpr(IS_E) f[0] = fe;
+	const V c3 = v_mul(v_set<V>(-3.0f), v_fma(ux, ux, v_fma(uy, uy, v_mul(uz, uz))));
+	const V ux3 = v_mul(v_set<V>(3.0f), ux), uy3 = v_mul(v_set<V>(3.0f), uy), uz3 = v_mul(v_set<V>(3.0f), uz);
+	V fxK = fx, fyK = fy, fzK = fz, uF = v_set<V>(0.0f); // Guo terms in storage units
+	if constexpr(VF) {
+		fxK = v_mul(v_set<V>(K), fx); fyK = v_mul(v_set<V>(K), fy); fzK = v_mul(v_set<V>(K), fz);
+		uF = v_mul(v_set<V>(-THIRD), v_fma(ux, fxK, v_fma(uy, fyK, v_mul(uz, fzK))));
+	}
+	{ // center: feq_0 = w_0 X; its difference to f_0 as one fused operation
+		const V X = v_fma(R, v_mul(v_set<V>(0.5f), c3), Rm1), w0 = v_set<V>(vs_w<Q>(0));
+		if constexpr(EMODE==1) f[0] = v_mul(w0, X);
 		else {
-			const float d0 = fe-f[0];
-			float g0 = !TRT ? fmaf(a.w, d0, f[0]) : fmaf(2.0f*a.hp, d0, f[0]);
-			if constexpr(VF) g0 = fmaf(!TRT ? a.c_tau : 2.0f*a.c_taup, (9.0f*vs_w<Q>(0))*uF, g0);
-			f[0] = g0;
+			const V d0 = v_fma(w0, X, v_neg(f[0]));
+			V g0 = v_fma(v_set<V>(!TRT ? a.w : 2.0f*a.hp), d0, f[0]);
+			if constexpr(VF) g0 = v_fma(v_set<V>(!TRT ? a.c_tau : 2.0f*a.c_taup), v_mul(v_set<V>(9.0f*vs_w<Q>(0)), uF), g0);
+			if constexpr(EMODE==2) f[0] = v_pick(g0, v_mul(w0, X), is_e); else f[0] = g0;
 		}
 	}
 	Unroll<1, Q, 2>::run([&](auto ic) {
 		constexpr int i = decltype(ic)::value;
 		const float wi = vs_w<Q>(i);
-		const float rw = wi*R;
-		const float uk = csum_fast<i>(ux3, uy3, uz3);
-		const float base = fmaf(0.5f*rw, fmaf(uk, uk, c3), wi*Rm1);
-		const float ea = fmaf(rw, uk, base), eb = fmaf(-rw, uk, base);
-		if constexpr(IS_E) { f[i] = ea; f[i+1] = eb; }
+		const V rw = v_mul(v_set<V>(wi), R);
+		const V uk = csum_v<i>(ux3, uy3, uz3);
+		const V base = v_fma(v_mul(v_set<V>(0.5f*wi), R), v_fma(uk, uk, c3), v_mul(v_set<V>(wi), Rm1));
+		const V ea = v_fma(rw, uk, base), eb = v_fma(v_neg(rw), uk, base);
+		if constexpr(EMODE==1) { f[i] = ea; f[i+1] = eb; }
 		else {
-			const float da = ea-f[i], db = eb-f[i+1];
-			float na, nb;
-			if constexpr(!TRT) { na = fmaf(a.w, da, f[i]); nb = fmaf(a.w, db, f[i+1]); }
+			const V da = v_sub(ea, f[i]), db = v_sub(eb, f[i+1]);
+			V na, nb;
+			if constexpr(!TRT) { na = v_fma(v_set<V>(a.w), da, f[i]); nb = v_fma(v_set<V>(a.w), db, f[i+1]); }
 			else {
-				const float t = a.hp*(da+db), dd = da-db;
-				na = f[i]+fmaf(a.hm, dd, t); nb = f[i+1]+fmaf(-a.hm, dd, t);
+				const V t = v_mul(v_set<V>(a.hp), v_add(da, db)), dd = v_sub(da, db);
+				na = v_add(f[i], v_fma(v_set<V>(a.hm), dd, t)); nb = v_add(f[i+1], v_fma(v_set<V>(-a.hm), dd, t));
 			}
 			if constexpr(VF) {
-				const float cf = csum_fast<i>(fxK, fyK, fzK);
-				const float gs = (18.0f*wi)*fmaf(cf, uk*THIRD, uF); // G_i + G_j  (c.u = uk/3)
-				const float gd = (6.0f*wi)*cf;                     // G_i - G_j
-				if constexpr(!TRT) { na = fmaf(0.5f*a.c_tau, gs+gd, na); nb = fmaf(0.5f*a.c_tau, gs-gd, nb); }
-				else { na += fmaf(a.c_taup, gs, a.c_taum*gd); nb += fmaf(a.c_taup, gs, -a.c_taum*gd); }
+				const V cf = csum_v<i>(fxK, fyK, fzK);
+				const V Y = v_fma(cf, v_mul(uk, v_set<V>(THIRD)), uF);
+				const V gd = v_mul(v_set<V>(6.0f*wi), cf);                     // G_i - G_j
+				if constexpr(!TRT) { // G_i = gs + gd and G_j = gs - gd, each one fused operation
+					na = v_fma(v_set<V>(0.5f*a.c_tau), v_fma(v_set<V>(18.0f*wi), Y, gd), na);
+					nb = v_fma(v_set<V>(0.5f*a.c_tau), v_fma(v_set<V>(18.0f*wi), Y, v_neg(gd)), nb);
+				} else {
+					const V gs = v_mul(v_set<V>(18.0f*wi), Y);                 // G_i + G_j  (c.u = uk/3)
+					const V m = v_mul(v_set<V>(a.c_taum), gd);
+					na = v_add(na, v_fma(v_set<V>(a.c_taup), gs, m)); nb = v_add(nb, v_fma(v_set<V>(a.c_taup), gs, v_neg(m)));
+				}
 			}
-			f[i] = na; f[i+1] = nb;
+			if constexpr(EMODE==2) { f[i] = v_pick(na, ea, is_e); f[i+1] = v_pick(nb, eb, is_e); }
+			else { f[i] = na; f[i+1] = nb; }
 		}
 	});
+}
+
+// ---------------------------------------------------------------- one cell (the scalar kernels)
+template<int Q, int EXT, int ST> __device__ __forceinline__ void cell_rho_u_fast(const StepArgs& a, const uint64_t n, const float* f, const bool is_e,
+                                                                                float& R, float& Rm1, float& inv, float& ux, float& uy, float& uz,
+                                                                                float& fx, float& fy, float& fz) {
+	cell_rho_u_v<Q, EXT, ST, float>(a, n, f, is_e, is_e, R, Rm1, inv, ux, uy, uz, fx, fy, fz);
 }
 template<int Q, bool TRT, bool VF, int ST> __device__ __forceinline__ void collide_fast(float* f, const float R, const float Rm1, const float ux, const float uy,
                                                                                       const float uz, const float fx, const float fy, const float fz,
                                                                                       const bool is_e, const StepArgs& a) {
-	if(is_e) collide_fast_t<Q, TRT, VF, ST, true>(f, R, Rm1, ux, uy, uz, fx, fy, fz, a);
-	else collide_fast_t<Q, TRT, VF, ST, false>(f, R, Rm1, ux, uy, uz, fx, fy, fz, a);
+	if(is_e) collide_v<Q, TRT, VF, ST, 1>(f, R, Rm1, ux, uy, uz, fx, fy, fz, is_e, a);
+	else collide_v<Q, TRT, VF, ST, 0>(f, R, Rm1, ux, uy, uz, fx, fy, fz, is_e, a);
 }
 
 } // namespace fx3d

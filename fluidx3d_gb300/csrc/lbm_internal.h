@@ -48,7 +48,7 @@ constexpr int ROW_TPB_MAX = 512; // threads per CTA of the row-staged stream_col
 
 // stream_collide implementation: one thread per cell with direct global loads/stores ("cells"), or
 // one CTA per x-row with the row's slots staged in shared memory by bulk copies ("rows")
-enum : int { PATH_AUTO = 0, PATH_CELLS = 1, PATH_ROWS = 2 };
+enum : int { PATH_AUTO = 0, PATH_CELLS = 1, PATH_ROWS = 2, PATH_PAIRS = 3, PATH_PIPE = 4 };
 // shared-memory plan of the row-staged kernel: bytes of one stage (one x-row's Q DDF rows + its flags)
 // and the number of stages; stages==0 if the lattice does not fit its constraints
 struct RowPlan { uint32_t stage_bytes, stages; size_t smem; };

@@ -5,6 +5,7 @@
 // Kernels and the reference functions they replace:
 //   k_initialize          src/kernel.cpp:1358-1430 initialize
 //   k_stream_collide      src/kernel.cpp:1454-1636 stream_collide
+//   k_stream_collide_pairs  the same, two x-adjacent cells per thread (fast arithmetic)
 //   k_update_fields       src/kernel.cpp:1794-1870 update_fields
 //   k_update_force_field  src/kernel.cpp:1873-1884 update_force_field
 #pragma once
@@ -12,6 +13,7 @@
 #include "lbm_internal.h"
 #include "lbm_bulk.cuh"
 #include "lbm_fast.cuh"
+#include "lbm_index32.cuh"
 
 namespace fx3d {
 
@@ -101,6 +103,242 @@ template<int Q, int ST, bool TRT, int EXT, bool FAST> __global__ void __launch_b
 	const bool is_e = EQ && flagsn_bo==TYPE_E;
 	cell_step<Q, ST, TRT, EXT, FAST>(f, a, n, is_e);
 	store_f<Q, ST, StepCodec<ST, FAST>>((T*)a.fi, g.N, n, nb, odd, f);
+}
+
+// Two x-adjacent cells (x0 even, x0+1) per thread, stepped together with packed FP32x2 arithmetic
+// (fast mode; grids with even Nx and fewer than 2^32 cells). A cell's own slots and the neighbour
+// slots of directions with c_x = 0 hold the two cells' values side by side at an even index, so they
+// move as one aligned 4-byte (FP16) or 8-byte (FP32) access; neighbour slots of directions with
+// c_x != 0 are one cell off and move as two scalar accesses. Each warp access so moves 128 bytes of
+// FP16 DDFs instead of 64, and the packed instructions halve the arithmetic issued per cell.
+// A pair with one solid (or gas) cell steps its other cell alone, on the one-cell path, which gives
+// bit-identical results (the arithmetic is the same code in float and float2 form).
+template<int ST> struct PairIO;
+template<> struct PairIO<ST_FP32> {
+	static __device__ __forceinline__ float2 load2(const float* p) { return *reinterpret_cast<const float2*>(p); }
+	static __device__ __forceinline__ void store2(float* p, const float2 v) { *reinterpret_cast<float2*>(p) = v; }
+};
+template<> struct PairIO<ST_FP16S> {
+	static __device__ __forceinline__ float2 load2(const uint16_t* p) { return __half22float2(*reinterpret_cast<const __half2*>(p)); }
+	static __device__ __forceinline__ void store2(uint16_t* p, const float2 v) { *reinterpret_cast<__half2*>(p) = __float22half2_rn(v); }
+};
+template<> struct PairIO<ST_FP16C> {
+	static __device__ __forceinline__ float2 load2(const uint16_t* p) { return make_float2(RawCodec<ST_FP16C>::decode(p[0]), RawCodec<ST_FP16C>::decode(p[1])); }
+	static __device__ __forceinline__ void store2(uint16_t* p, const float2 v) { p[0] = RawCodec<ST_FP16C>::encode(v.x); p[1] = RawCodec<ST_FP16C>::encode(v.y); }
+};
+
+template<int Q, int ST, typename T> __device__ __forceinline__ void load_pair(const T* __restrict__ fi, const uint64_t N, const Steps32& sa, const Steps32& sb,
+                                                                              const bool odd, float2* f) {
+	typedef RawCodec<ST> CD;
+	const uint64_t e = odd ? 0ull : N;
+	f[0] = PairIO<ST>::load2(fi+sa.n);
+	Unroll<1, Q, 2>::run([&](auto ic) {
+		constexpr int i = decltype(ic)::value;
+		const T* pa = fi+((uint64_t)i*N+e);
+		const T* pb = fi+((uint64_t)(i+1)*N-e);
+		f[i] = PairIO<ST>::load2(pa+sa.n);
+		if constexpr(vs_c(0, i)==0) f[i+1] = PairIO<ST>::load2(pb+sa.template j<i>());
+		else f[i+1] = make_float2(CD::decode(pb[sa.template j<i>()]), CD::decode(pb[sb.template j<i>()]));
+	});
+}
+template<int Q, int ST, typename T> __device__ __forceinline__ void store_pair(T* __restrict__ fi, const uint64_t N, const Steps32& sa, const Steps32& sb,
+                                                                               const bool odd, const float2* f) {
+	typedef RawCodec<ST> CD;
+	const uint64_t e = odd ? 0ull : N;
+	PairIO<ST>::store2(fi+sa.n, f[0]);
+	Unroll<1, Q, 2>::run([&](auto ic) {
+		constexpr int i = decltype(ic)::value;
+		T* pa = fi+((uint64_t)i*N+e);
+		T* pb = fi+((uint64_t)(i+1)*N-e);
+		if constexpr(vs_c(0, i)==0) PairIO<ST>::store2(pb+sa.template j<i>(), f[i]);
+		else { pb[sa.template j<i>()] = CD::encode(f[i].x); pb[sb.template j<i>()] = CD::encode(f[i].y); }
+		PairIO<ST>::store2(pa+sa.n, f[i+1]);
+	});
+}
+
+inline dim3 pair_grid(const GridDesc& g) { return dim3((g.NxNy/2u+BLOCK-1u)/BLOCK, g.Nz, 1u); }
+inline bool pairs_supported(const GridDesc& g) { return g.Nx%2u==0u && g.N<=0xFFFFFFFFull; }
+
+#ifndef FX3D_PAIRS_MIN_BLOCKS
+#define FX3D_PAIRS_MIN_BLOCKS 3 // resident 256-thread blocks per SM the register budget is sized for (80 registers)
+#endif
+template<int Q, int ST, bool TRT, int EXT> __global__ void __launch_bounds__(BLOCK, FX3D_PAIRS_MIN_BLOCKS) k_stream_collide_pairs(const StepArgs a) {
+	typedef typename Codec<ST>::T T;
+	constexpr bool EQ = (EXT&EXT_EQ)!=0, VF = (EXT&EXT_VF)!=0;
+	const Grid& g = grid_of(a.g);
+	const uint32_t xy = 2u*(blockIdx.x*(uint32_t)BLOCK+threadIdx.x);
+	if(xy>=g.NxNy) return;
+	const uint32_t z = blockIdx.y, y = div_nx(g, xy), x = xy-y*g.Nx;
+	const uint32_t n = z*g.NxNy+xy;
+	const uint16_t fl = *reinterpret_cast<const uint16_t*>(a.flags+n); // both cells' flags (n even)
+	const uint32_t fa = fl&0xFFu, fb = fl>>8;
+	const bool skip_a = (fa&TYPE_BO)==TYPE_S||(fa&TYPE_SU)==TYPE_G, skip_b = (fb&TYPE_BO)==TYPE_S||(fb&TYPE_SU)==TYPE_G;
+	if(skip_a&&skip_b) return;
+	const bool odd = (a.t&1ull)!=0ull;
+	if(skip_a||skip_b) { // one cell of the pair steps alone
+		const uint32_t c = skip_a ? 1u : 0u;
+		const Steps32 s(g, x+c, y, z, n+c);
+		float f[Q];
+		load_f32<Q, RawCodec<ST>>((const T*)a.fi, g.N, s, odd, f);
+		cell_step<Q, ST, TRT, EXT, true>(f, a, n+c, EQ && ((skip_a ? fb : fa)&TYPE_BO)==TYPE_E);
+		store_f32<Q, RawCodec<ST>>((T*)a.fi, g.N, s, odd, f);
+		return;
+	}
+	const Steps32 sa(g, x, y, z, n), sb(g, x+1u, y, z, n+1u);
+	float2 f[Q];
+	load_pair<Q, ST>((const T*)a.fi, g.N, sa, sb, odd, f);
+	const Bool2 is_e{EQ && (fa&TYPE_BO)==TYPE_E, EQ && (fb&TYPE_BO)==TYPE_E};
+	const bool any_e = is_e.x||is_e.y;
+	float2 R, Rm1, inv, ux, uy, uz, fx, fy, fz;
+	cell_rho_u_v<Q, EXT, ST, float2>(a, n, f, is_e, any_e, R, Rm1, inv, ux, uy, uz, fx, fy, fz);
+	if(any_e) collide_v<Q, TRT, VF, ST, 2>(f, R, Rm1, ux, uy, uz, fx, fy, fz, is_e, a);
+	else collide_v<Q, TRT, VF, ST, 0>(f, R, Rm1, ux, uy, uz, fx, fy, fz, is_e, a);
+	store_pair<Q, ST>((T*)a.fi, g.N, sa, sb, odd, f);
+}
+
+// Two-cell kernel with per-thread prefetch. A thread walks the pairs (x0, y, z) of a column of z
+// planes; while it steps one pair, the DDF words of the next S-1 pairs are already in flight as
+// per-thread cp.async copies into its own shared-memory slots (item k of stage s at
+// smem[(s*ITEMS + k)*BLOCK + thread]), so every warp keeps loads outstanding through its compute and
+// store phases without holding them in registers, and no block-wide barrier is needed. Per pair the
+// items are: the aligned 4-byte flags word holding both cells' flags, the rest slot, the own slots
+// of each direction pair, and for each neighbour slot either one aligned pair word (c_x = 0) or two
+// words (c_x != 0): for FP16 the aligned words holding the first cell's value in their upper half
+// (index j-1, j odd) and the second cell's value in their lower half (j even), for FP32 the two
+// values themselves. Values next to them belong to other cells and are read but never used.
+// Results are bit-identical to the plain two-cell kernel: only where the loads land differs.
+template<int Q> __host__ __device__ constexpr int pair_nx0() { int c = 0; for(int i=1; i<Q; i+=2) if(vs_c(0, i)==0) c++; return c; }
+template<int Q> __host__ __device__ constexpr int pair_items() { return 2+(Q-1)/2+pair_nx0<Q>()+2*((Q-1)/2-pair_nx0<Q>()); }
+template<int Q> __host__ __device__ constexpr int pair_b_item(const int i) { // first item of the neighbour slot of pair (i, i+1)
+	int k = 2+(Q-1)/2;
+	for(int p=1; p<i; p+=2) k += vs_c(0, p)==0 ? 1 : 2;
+	return k;
+}
+
+template<int Q, int ST, typename T> __device__ __forceinline__ void issue_pair(const T* __restrict__ fi, const uint8_t* __restrict__ flags, const uint64_t N,
+                                                                               const Steps32& sa, const Steps32& sb, const bool odd, const uint32_t s0) {
+	constexpr uint32_t W = 2u*sizeof(T), STRIDE = BLOCK*W; // item size, distance of consecutive items
+	auto cpw = [](const uint32_t d, const T* p) { if constexpr(W==4u) cp_async_4(d, p); else cp_async_8(d, p); };
+	const uint64_t e = odd ? 0ull : N;
+	cp_async_4(s0, flags+(sa.n&~3u));
+	cpw(s0+STRIDE, fi+sa.n);
+	Unroll<1, Q, 2>::run([&](auto ic) {
+		constexpr int i = decltype(ic)::value;
+		constexpr uint32_t ka = 2u+(uint32_t)(i-1)/2u, kb = (uint32_t)pair_b_item<Q>(i);
+		const T* pa = fi+((uint64_t)i*N+e);
+		const T* pb = fi+((uint64_t)(i+1)*N-e);
+		cpw(s0+ka*STRIDE, pa+sa.n);
+		if constexpr(vs_c(0, i)==0) cpw(s0+kb*STRIDE, pb+sa.template j<i>());
+		else if constexpr(W==4u) { cp_async_4(s0+kb*STRIDE, pb+(sa.template j<i>()-1u)); cp_async_4(s0+(kb+1u)*STRIDE, pb+sb.template j<i>()); }
+		else { cp_async_4(s0+kb*STRIDE, pb+sa.template j<i>()); cp_async_4(s0+(kb+1u)*STRIDE, pb+sb.template j<i>()); }
+	});
+}
+
+// the pair's values from its staged items (item k of this thread at w[k*BLOCK])
+template<int ST> struct PairStage;
+template<> struct PairStage<ST_FP32> {
+	typedef float2 W;
+	static __device__ __forceinline__ float2 pair(const W* w, const int k) { return w[k*BLOCK]; }
+	static __device__ __forceinline__ float2 split(const W* w, const int k) { return make_float2(w[k*BLOCK].x, w[(k+1)*BLOCK].x); }
+	static __device__ __forceinline__ uint32_t flags(const W* w) { return __float_as_uint(w[0].x); }
+};
+template<> struct PairStage<ST_FP16S> {
+	typedef uint32_t W;
+	static __device__ __forceinline__ float2 pair(const W* w, const int k) { return __half22float2(__halves2half2(__ushort_as_half((uint16_t)(w[k*BLOCK]&0xFFFFu)), __ushort_as_half((uint16_t)(w[k*BLOCK]>>16)))); }
+	static __device__ __forceinline__ float2 split(const W* w, const int k) { // upper half of item k, lower half of item k+1
+		const uint32_t v = __byte_perm(w[k*BLOCK], w[(k+1)*BLOCK], 0x5432u);
+		return __half22float2(__halves2half2(__ushort_as_half((uint16_t)(v&0xFFFFu)), __ushort_as_half((uint16_t)(v>>16))));
+	}
+	static __device__ __forceinline__ uint32_t flags(const W* w) { return w[0]; }
+};
+template<> struct PairStage<ST_FP16C> { // the two codes read as 16-bit halves of the staged words
+	typedef uint32_t W;
+	static __device__ __forceinline__ const uint16_t* h(const W* w, const int k) { return reinterpret_cast<const uint16_t*>(w+k*BLOCK); }
+	static __device__ __forceinline__ float2 pair(const W* w, const int k) { return make_float2(RawCodec<ST_FP16C>::decode(h(w, k)[0]), RawCodec<ST_FP16C>::decode(h(w, k)[1])); }
+	static __device__ __forceinline__ float2 split(const W* w, const int k) { return make_float2(RawCodec<ST_FP16C>::decode(h(w, k)[1]), RawCodec<ST_FP16C>::decode(h(w, k+1)[0])); }
+	static __device__ __forceinline__ uint32_t flags(const W* w) { return w[0]; }
+};
+template<int Q, int ST> __device__ __forceinline__ void read_pair(const typename PairStage<ST>::W* w, float2* f) {
+	f[0] = PairStage<ST>::pair(w, 1);
+	Unroll<1, Q, 2>::run([&](auto ic) {
+		constexpr int i = decltype(ic)::value;
+		f[i] = PairStage<ST>::pair(w, 2+(i-1)/2);
+		if constexpr(vs_c(0, i)==0) f[i+1] = PairStage<ST>::pair(w, pair_b_item<Q>(i));
+		else f[i+1] = PairStage<ST>::split(w, pair_b_item<Q>(i));
+	});
+}
+
+#ifndef FX3D_PIPE_MIN_BLOCKS
+#define FX3D_PIPE_MIN_BLOCKS 3
+#endif
+#ifndef FX3D_PIPE_STAGES
+#define FX3D_PIPE_STAGES 2
+#endif
+#ifndef FX3D_PIPE_Z_CHUNK
+#define FX3D_PIPE_Z_CHUNK 8
+#endif
+constexpr int PIPE_STAGES = FX3D_PIPE_STAGES; // pairs in flight per thread: PIPE_STAGES-1 ahead of the one stepped
+inline uint32_t pipe_z_chunk(const GridDesc& g) { return g.Nz<(uint32_t)FX3D_PIPE_Z_CHUNK ? g.Nz : (uint32_t)FX3D_PIPE_Z_CHUNK; } // z planes per thread
+template<int Q, int ST> inline size_t pipe_smem(const int stages) { return (size_t)stages*pair_items<Q>()*BLOCK*2u*sizeof(typename Codec<ST>::T); }
+
+template<int Q, int ST, bool TRT, int EXT, int S> __global__ void __launch_bounds__(BLOCK, FX3D_PIPE_MIN_BLOCKS) k_stream_collide_pairs_pipe(const StepArgs a, const uint32_t zc) {
+	typedef typename Codec<ST>::T T;
+	typedef typename PairStage<ST>::W SW;
+	constexpr bool EQ = (EXT&EXT_EQ)!=0, VF = (EXT&EXT_VF)!=0;
+	constexpr int ITEMS = pair_items<Q>();
+	extern __shared__ __align__(16) uint8_t pipe_smem_raw[];
+	const Grid& g = grid_of(a.g);
+	const uint32_t xy = 2u*(blockIdx.x*(uint32_t)BLOCK+threadIdx.x);
+	if(xy>=g.NxNy) return; // threads never wait on each other
+	const uint32_t y = div_nx(g, xy), x = xy-y*g.Nx;
+	const uint32_t z0 = blockIdx.y*zc, z1 = min(z0+zc, g.Nz);
+	const bool odd = (a.t&1ull)!=0ull;
+	SW* const w0 = reinterpret_cast<SW*>(pipe_smem_raw)+threadIdx.x;
+	const uint32_t s0 = smem_u32(w0);
+	auto issue = [&](const uint32_t z, const int stage) {
+		const uint32_t n = z*g.NxNy+xy;
+		const Steps32 sa(g, x, y, z, n), sb(g, x+1u, y, z, n+1u);
+		issue_pair<Q, ST>((const T*)a.fi, a.flags, g.N, sa, sb, odd, s0+(uint32_t)(stage*ITEMS*BLOCK)*(uint32_t)sizeof(SW));
+	};
+	#pragma unroll
+	for(int s=0; s<S-1; s++) {
+		if(z0+(uint32_t)s<z1) issue(z0+(uint32_t)s, s);
+		cp_async_commit();
+	}
+	int stage = 0;
+	for(uint32_t z=z0; z<z1; z++) {
+		const int ahead = stage+S-1<S ? stage+S-1 : stage-1; // the stage the previous pair used
+		if(z+(uint32_t)(S-1)<z1) issue(z+(uint32_t)(S-1), ahead);
+		cp_async_commit();
+		cp_async_wait<S-1>();
+		const SW* w = w0+stage*ITEMS*BLOCK;
+		stage = stage+1<S ? stage+1 : 0;
+		const uint32_t n = z*g.NxNy+xy;
+		const uint32_t fl = PairStage<ST>::flags(w)>>((n&3u)*8u); // both cells' flags (n even)
+		const uint32_t fa = fl&0xFFu, fb = (fl>>8)&0xFFu;
+		const bool skip_a = (fa&TYPE_BO)==TYPE_S||(fa&TYPE_SU)==TYPE_G, skip_b = (fb&TYPE_BO)==TYPE_S||(fb&TYPE_SU)==TYPE_G;
+		if(skip_a&&skip_b) continue;
+		float2 f[Q];
+		read_pair<Q, ST>(w, f);
+		if(skip_a||skip_b) { // one cell of the pair steps alone
+			const uint32_t c = skip_a ? 1u : 0u;
+			const Steps32 s(g, x+c, y, z, n+c);
+			float f1[Q];
+			#pragma unroll
+			for(int k=0; k<Q; k++) f1[k] = c ? f[k].y : f[k].x;
+			cell_step<Q, ST, TRT, EXT, true>(f1, a, n+c, EQ && ((skip_a ? fb : fa)&TYPE_BO)==TYPE_E);
+			store_f32<Q, RawCodec<ST>>((T*)a.fi, g.N, s, odd, f1);
+			continue;
+		}
+		const Steps32 sa(g, x, y, z, n), sb(g, x+1u, y, z, n+1u);
+		const Bool2 is_e{EQ && (fa&TYPE_BO)==TYPE_E, EQ && (fb&TYPE_BO)==TYPE_E};
+		const bool any_e = is_e.x||is_e.y;
+		float2 R, Rm1, inv, ux, uy, uz, fx, fy, fz;
+		cell_rho_u_v<Q, EXT, ST, float2>(a, n, f, is_e, any_e, R, Rm1, inv, ux, uy, uz, fx, fy, fz);
+		if(any_e) collide_v<Q, TRT, VF, ST, 2>(f, R, Rm1, ux, uy, uz, fx, fy, fz, is_e, a);
+		else collide_v<Q, TRT, VF, ST, 0>(f, R, Rm1, ux, uy, uz, fx, fy, fz, is_e, a);
+		store_pair<Q, ST>((T*)a.fi, g.N, sa, sb, odd, f);
+	}
 }
 
 // Row-staged stream_collide. At either parity the cells of one x-row (y,z) own exactly Q whole
@@ -284,8 +522,8 @@ template<int Q, int ST> __global__ void __launch_bounds__(BLOCK) k_update_force_
 // ---------------------------------------------------------------- dispatch
 inline dim3 cell_grid(const GridDesc& g) { return dim3((g.NxNy+BLOCK-1u)/BLOCK, g.Nz, 1u); }
 
-template<int ST, int Q, bool TRT, int EXT, bool FAST> inline cudaError_t sc_launch_t(const StepArgs& a, const bool rows, cudaStream_t s) {
-	if(rows) {
+template<int ST, int Q, bool TRT, int EXT, bool FAST> inline cudaError_t sc_launch_t(const StepArgs& a, const int kind, cudaStream_t s) {
+	if(kind==PATH_ROWS) {
 		const RowPlan plan = row_plan(Q, ST, a.g.Nx, a.g.Ny, a.g.Nz);
 		if(plan.stages==0u) return cudaErrorInvalidConfiguration;
 		auto kernel = k_stream_collide_rows<Q, ST, TRT, EXT, FAST>;
@@ -298,32 +536,55 @@ template<int ST, int Q, bool TRT, int EXT, bool FAST> inline cudaError_t sc_laun
 		int grid = persistent_grid((const void*)kernel, tpb, plan.smem);
 		if((uint64_t)grid>rows_total) grid = (int)rows_total;
 		kernel<<<grid, tpb, plan.smem, s>>>(a, plan.stages);
+	} else if(kind==PATH_PAIRS||kind==PATH_PIPE) {
+		if constexpr(FAST) {
+			if(a.fi_dst!=a.fi||!pairs_supported(a.g)) return cudaErrorInvalidValue; // in place, even Nx, N < 2^32
+			if(kind==PATH_PAIRS) k_stream_collide_pairs<Q, ST, TRT, EXT><<<pair_grid(a.g), BLOCK, 0, s>>>(a);
+			else {
+				constexpr int S = PIPE_STAGES;
+				auto kernel = k_stream_collide_pairs_pipe<Q, ST, TRT, EXT, S>;
+				const size_t smem = pipe_smem<Q, ST>(S);
+				if(smem>48u*1024u) {
+					const cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+					if(e!=cudaSuccess) return e;
+				}
+				const uint32_t zc = pipe_z_chunk(a.g);
+				kernel<<<dim3(pair_grid(a.g).x, (a.g.Nz+zc-1u)/zc, 1u), BLOCK, smem, s>>>(a, zc);
+			}
+		} else {
+			return cudaErrorInvalidConfiguration; // the packed kernel has fast arithmetic only
+		}
 	} else {
 		if(a.fi_dst!=a.fi) return cudaErrorInvalidValue; // one thread per cell steps in place only
 		k_stream_collide<Q, ST, TRT, EXT, FAST><<<cell_grid(a.g), BLOCK, 0, s>>>(a);
 	}
 	return cudaGetLastError();
 }
-template<int ST, int Q, bool TRT, int EXT> inline cudaError_t sc_launch(const StepArgs& a, const bool rows, const bool fast, cudaStream_t s) {
-	return fast ? sc_launch_t<ST, Q, TRT, EXT, true>(a, rows, s) : sc_launch_t<ST, Q, TRT, EXT, false>(a, rows, s);
+template<int ST, int Q, bool TRT, int EXT> inline cudaError_t sc_launch(const StepArgs& a, const int kind, const bool fast, cudaStream_t s) {
+	return fast ? sc_launch_t<ST, Q, TRT, EXT, true>(a, kind, s) : sc_launch_t<ST, Q, TRT, EXT, false>(a, kind, s);
 }
-template<int ST, int Q, bool TRT> inline cudaError_t sc_ext(const int ext, const StepArgs& a, const bool rows, const bool fast, cudaStream_t s) {
+template<int ST, int Q, bool TRT> inline cudaError_t sc_ext(const int ext, const StepArgs& a, const int kind, const bool fast, cudaStream_t s) {
 	switch(ext) {
-		case 0:                        return sc_launch<ST, Q, TRT, 0>(a, rows, fast, s);
-		case EXT_VF:                   return sc_launch<ST, Q, TRT, EXT_VF>(a, rows, fast, s);
-		case EXT_VF|EXT_FF:            return sc_launch<ST, Q, TRT, EXT_VF|EXT_FF>(a, rows, fast, s);
-		case EXT_EQ:                   return sc_launch<ST, Q, TRT, EXT_EQ>(a, rows, fast, s);
-		case EXT_EQ|EXT_VF:            return sc_launch<ST, Q, TRT, EXT_EQ|EXT_VF>(a, rows, fast, s);
-		case EXT_EQ|EXT_VF|EXT_FF:     return sc_launch<ST, Q, TRT, EXT_EQ|EXT_VF|EXT_FF>(a, rows, fast, s);
+		case 0:                        return sc_launch<ST, Q, TRT, 0>(a, kind, fast, s);
+		case EXT_VF:                   return sc_launch<ST, Q, TRT, EXT_VF>(a, kind, fast, s);
+		case EXT_VF|EXT_FF:            return sc_launch<ST, Q, TRT, EXT_VF|EXT_FF>(a, kind, fast, s);
+		case EXT_EQ:                   return sc_launch<ST, Q, TRT, EXT_EQ>(a, kind, fast, s);
+		case EXT_EQ|EXT_VF:            return sc_launch<ST, Q, TRT, EXT_EQ|EXT_VF>(a, kind, fast, s);
+		case EXT_EQ|EXT_VF|EXT_FF:     return sc_launch<ST, Q, TRT, EXT_EQ|EXT_VF|EXT_FF>(a, kind, fast, s);
 		default: return cudaErrorInvalidValue;
 	}
 }
 template<int ST> cudaError_t launch_stream_collide_t(const Variant& v, const StepArgs& a, const int path, cudaStream_t s) {
+	// automatic choice (measured on 512x256x256): for fast arithmetic in place the two-cell kernel,
+	// with per-thread prefetch for 16-bit storage (FP32 moves enough bytes per access without it);
+	// otherwise one thread per cell in place, and the row-staged kernel for steps into another array
 	const bool rows_ok = row_plan(v.q, ST, a.g.Nx, a.g.Ny, a.g.Nz).stages!=0u;
-	if(path==PATH_ROWS && !rows_ok) return cudaErrorInvalidConfiguration;
-	const bool rows = path==PATH_ROWS || (path==PATH_AUTO && rows_ok);
-	if(v.q==19) return v.trt ? sc_ext<ST, 19, true>(v.ext, a, rows, v.fast, s) : sc_ext<ST, 19, false>(v.ext, a, rows, v.fast, s);
-	if(v.q==27) return v.trt ? sc_ext<ST, 27, true>(v.ext, a, rows, v.fast, s) : sc_ext<ST, 27, false>(v.ext, a, rows, v.fast, s);
+	const bool pairs_ok = v.fast && pairs_supported(a.g) && a.fi_dst==a.fi;
+	int kind = path;
+	if(path==PATH_AUTO) kind = pairs_ok ? (ST==ST_FP32 ? PATH_PAIRS : PATH_PIPE) : a.fi_dst!=a.fi ? PATH_ROWS : PATH_CELLS;
+	if((kind==PATH_ROWS && !rows_ok) || ((kind==PATH_PAIRS||kind==PATH_PIPE) && !pairs_ok)) return cudaErrorInvalidConfiguration;
+	if(v.q==19) return v.trt ? sc_ext<ST, 19, true>(v.ext, a, kind, v.fast, s) : sc_ext<ST, 19, false>(v.ext, a, kind, v.fast, s);
+	if(v.q==27) return v.trt ? sc_ext<ST, 27, true>(v.ext, a, kind, v.fast, s) : sc_ext<ST, 27, false>(v.ext, a, kind, v.fast, s);
 	return cudaErrorInvalidValue;
 }
 

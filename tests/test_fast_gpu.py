@@ -9,6 +9,10 @@ and its error against the FP64 scheme stays within 1.6x the exact FP32 scheme's 
 Over the 1000-step 64^3 Taylor-Green run the exact FP32 scheme itself is 1.3e-5 (max-norm)
 from FP64, so there the fast mode is held to the same FP32 rounding floor: 3e-5 from exact and
 2x the exact scheme's error from FP64.
+
+The two-cell packed kernels ("pairs", and "pipe" with per-thread prefetch) run the same arithmetic
+as the one-cell kernel in float2 form, with every operation rounded explicitly, so all three are
+held to bit-identical DDFs.
 """
 import os
 
@@ -18,6 +22,7 @@ import pytest
 import oracle
 import lbm_cases as LC
 from test_forward_gpu import make_gpu, make_oracle
+from fluidx3d_gb300 import LBM, setups as S
 
 pytestmark = pytest.mark.gpu
 
@@ -32,7 +37,7 @@ def errors(lbm, o):
     return drho, du
 
 
-@pytest.fixture(params=["rows", "cells"])
+@pytest.fixture(params=["rows", "cells", "pairs", "pipe"])
 def path(request, monkeypatch):
     monkeypatch.setenv("FX3D_STREAM_COLLIDE_PATH", request.param)
     return request.param
@@ -104,3 +109,47 @@ def test_fast_force_reduction_close_to_exact(gpu):
         b.run(30)
         fa, fb = a.object_force(0x41), b.object_force(0x41)
         assert np.allclose(fa, fb, rtol=1e-4, atol=1e-9)
+
+
+@pytest.mark.parametrize("case", LC.CASES + [LC.TGV64], ids=[c.name for c in LC.CASES] + [LC.TGV64.name])
+def test_pairs_bit_identical_to_one_cell_kernel(case, gpu, monkeypatch):
+    out = {}
+    for p in ("cells", "pairs", "pipe"):
+        monkeypatch.setenv("FX3D_STREAM_COLLIDE_PATH", p)
+        with make_gpu(case, arithmetic="fast") as lbm:
+            lbm.run(case.steps if case.steps < 200 else 200)
+            out[p] = lbm.read_ddfs()
+    assert np.array_equal(out["cells"], out["pairs"])
+    assert np.array_equal(out["cells"], out["pipe"])
+
+
+@pytest.mark.parametrize("q", [19, 27])
+@pytest.mark.parametrize("storage", ["fp32", "fp16s", "fp16c"])
+def test_pipe_ragged_z_chunks(q, storage, gpu, monkeypatch):
+    """37 z planes: the prefetching kernel's columns of 16 planes end in a ragged chunk; a sphere and
+    walls give pairs with one solid cell, TYPE_E inlet/outlet pairs with one equilibrium cell."""
+    Nx, Ny, Nz = 32, 10, 37
+    f = S.sphere_channel(Nx, Ny, Nz, u_in=0.05, radius=4.0, center=(11.0, 5.0, 18.0))
+    out = {}
+    for p in ("cells", "pipe"):
+        monkeypatch.setenv("FX3D_STREAM_COLLIDE_PATH", p)
+        with LBM(Nx, Ny, Nz, 0.03, velocity_set=q, collision="trt", storage=storage, extensions=("eq",), arithmetic="fast") as lbm:
+            lbm.rho.data[:], lbm.u.data[:], lbm.flags.data[:] = f["rho"], f["u"], f["flags"]
+            lbm.run(23)
+            out[p] = lbm.read_ddfs()
+    assert np.array_equal(out["cells"], out["pipe"])
+
+
+def test_pairs_need_even_nx(gpu, monkeypatch):
+    from fluidx3d_gb300 import LBM, LBMError
+    monkeypatch.setenv("FX3D_STREAM_COLLIDE_PATH", "pairs")
+    with LBM(15, 8, 6, 0.05, storage="fp16s") as lbm:
+        with pytest.raises(LBMError):
+            lbm.run(1)
+    monkeypatch.delenv("FX3D_STREAM_COLLIDE_PATH")
+    with LBM(15, 8, 6, 0.05, storage="fp16s") as a:  # automatic choice falls back to one cell per thread
+        a.run(3)
+        monkeypatch.setenv("FX3D_STREAM_COLLIDE_PATH", "cells")
+        with LBM(15, 8, 6, 0.05, storage="fp16s") as b:
+            b.run(3)
+            assert np.array_equal(a.read_ddfs(), b.read_ddfs())
