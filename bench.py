@@ -35,6 +35,16 @@ sys.path.insert(0, ROOT)
 
 WORKLOAD = dict(name="sphere_channel_512x256x256_d3q19_trt_fp16s", Nx=512, Ny=256, Nz=256, q=19, collision="trt", storage="fp16s",
                 extensions=("eq",), u_in=0.075, radius=32.0, center=(128.0, 128.0, 128.0), nu=0.075 * 64.0 / 100.0)
+# the kernel the solver picks for this workload (fast arithmetic, FP16S storage, even Nx)
+KERNEL = "k_stream_collide_pairs_pipe<19,FP16S,TRT,EQ> (two cells per thread, packed FP32x2, per-thread cp.async prefetch)"
+
+
+def set_size(spec):
+    """--size NXxNYxNZ: the same channel scaled (sphere radius and centre with Ny), for profiling captures."""
+    Nx, Ny, Nz = (int(v) for v in spec.lower().split("x"))
+    k = Ny / 256.0
+    WORKLOAD.update(name=f"sphere_channel_{Nx}x{Ny}x{Nz}_d3q19_trt_fp16s", Nx=Nx, Ny=Ny, Nz=Nz, radius=32.0 * k,
+                    center=(128.0 * k, 128.0 * k, 128.0 * k), nu=0.075 * 64.0 * k / 100.0)
 METRIC = "MLUPs/s"
 FALLBACK_HBM_GBS = 6800.0
 
@@ -116,7 +126,8 @@ def dist_setup(n_gpus):
     import torch
     import torch.distributed as dist
     rank, local = int(os.environ["RANK"]), int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
+    if torch.cuda.is_available():
+        torch.cuda.set_device(local)
     dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     return dist, rank, world, local
 
@@ -130,7 +141,7 @@ def max_over_ranks(dist, x):
     if dist is None:
         return x
     import torch
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
@@ -263,7 +274,7 @@ def run_gpu_arm(args):
                    "l2": "inputs larger than L2 (1.27 GB DDFs per step), no flush",
                    "bytes_per_cell_step": bpc},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "peak_source": f"{peak_kind} hbm_gbs", "kernel": "k_stream_collide<19,FP16S,TRT,EQ>"},
+                     "traffic": traffic, "peak_source": f"{peak_kind} hbm_gbs", "kernel": KERNEL},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d / K, "d2h_bytes_per_step": d2h / K,
                 "job": f"upload rho/u/flags + initialize + {K} steps + update_fields + download rho/u"},
@@ -283,7 +294,10 @@ def main():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU-baseline work")
+    ap.add_argument("--size", default=None, help="NXxNYxNZ instead of 512x256x256 (profiling captures of a small case)")
     args = ap.parse_args()
+    if args.size:
+        set_size(args.size)
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     if args.impl == "reference":

@@ -300,8 +300,8 @@ int lbm_domain_create(const lbm_config* c, lbm_domain** out) {
 	d->w = lbm_relaxation_rate(c->nu);
 	d->rates = make_rates(d->w);
 	// stream_collide implementation: FX3D_STREAM_COLLIDE_PATH=cells|rows|pairs|pipe forces one (diagnostics
-	// and tests); the default takes a two-cell packed kernel for fast arithmetic where the lattice
-	// allows it (even Nx, fewer than 2^32 cells; with per-thread prefetch for 16-bit storage), else
+	// and tests); the default takes the two-cell packed kernel with per-thread prefetch for fast
+	// arithmetic on 16-bit storage where the lattice allows it (even Nx, fewer than 2^32 cells), else
 	// one thread per cell
 	if(const char* p = std::getenv("FX3D_STREAM_COLLIDE_PATH")) {
 		if(!std::strcmp(p, "cells")) d->path = PATH_CELLS;

@@ -5,8 +5,8 @@
 //   * DDFs stay in storage units: FP16S values are used as stored (2^15 times the DDF), so loads and
 //     stores are a bare conversion; the density carries the same factor K (R = K*rho), the Guo force
 //     terms are scaled by K and the velocity, a ratio, needs no rescaling;
-//   * one reciprocal of R per cell instead of four divisions (the velocity gets one Newton
-//     correction); rho-1 is the plain sum of the shifted DDFs (the shift is added after summing, as
+//   * one reciprocal of R per cell instead of four divisions (hardware approximation plus one
+//     Newton step; the velocity gets one more Newton correction); rho-1 is the plain sum of the shifted DDFs (the shift is added after summing, as
 //     the reference intends with DDF shifting);
 //   * moments from pair sums and pair differences (f_i+f_j, f_i-f_j for opposite i,j);
 //   * equilibrium of an opposite pair from one shared base term: feq_{i,j} = base +- rho w_i u_k;
@@ -16,7 +16,7 @@
 //   * Guo terms of a pair from G_i+G_j = 18 w (c.F)(c.u) + 18 w uF and G_i-G_j = 6 w (c.F).
 //
 // The arithmetic is written once for a value type V: float (one cell) or float2 (two cells, issued
-// as the packed FP32 instructions of sm_100 and later: add/mul.rn.f32x2, __ffma2_rn). Every
+// as the packed FP32 instructions of sm_100 and later: __fadd2_rn, __fmul2_rn, __ffma2_rn). Every
 // operation is explicitly rounded and the packed forms round each component exactly as the scalar
 // ones. ptxas fuses a packed multiply whose only use is a packed add into a packed multiply-add
 // even with explicit .rn modifiers (the scalar __fmul_rn/__fadd_rn are never fused), so no
@@ -65,20 +65,8 @@ __device__ __forceinline__ float v_sub(const float a, const float b) { return __
 __device__ __forceinline__ float v_mul(const float a, const float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ float v_fma(const float a, const float b, const float c) { return __fmaf_rn(a, b, c); }
 __device__ __forceinline__ float v_neg(const float a) { return -a; }
-// packed add and multiply as PTX with an explicit .rn rounding modifier: the compiler never fuses
-// those into a multiply-add (as __fmul_rn/__fadd_rn), which keeps float2 results equal to float ones
-__device__ __forceinline__ float2 v_add(const float2 a, const float2 b) {
-	float2 d;
-	asm("{\n\t.reg .b64 ra, rb, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\tadd.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
-	    : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
-	return d;
-}
-__device__ __forceinline__ float2 v_mul(const float2 a, const float2 b) {
-	float2 d;
-	asm("{\n\t.reg .b64 ra, rb, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\tmul.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
-	    : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
-	return d;
-}
+__device__ __forceinline__ float2 v_add(const float2 a, const float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 v_mul(const float2 a, const float2 b) { return __fmul2_rn(a, b); }
 __device__ __forceinline__ float2 v_neg(const float2 a) { return make_float2(-a.x, -a.y); }
 __device__ __forceinline__ float2 v_sub(const float2 a, const float2 b) { return v_add(a, v_neg(b)); } // a-b == a+(-b) in IEEE
 __device__ __forceinline__ float2 v_fma(const float2 a, const float2 b, const float2 c) { return __ffma2_rn(a, b, c); }
@@ -97,7 +85,12 @@ __device__ __forceinline__ void v_load(float& v, const float* p) { v = *p; }
 __device__ __forceinline__ void v_load(float2& v, const float* p) { v = *reinterpret_cast<const float2*>(p); }
 __device__ __forceinline__ float v_clampc(const float x) { return fminf(fmaxf(x, -DEF_C), DEF_C); }
 template<class V> __device__ __forceinline__ V v_clamp(const V x) { return v_map(x, [](const float t) { return v_clampc(t); }); }
-template<class V> __device__ __forceinline__ V v_rcp(const V x) { return v_map(x, [](const float t) { return __frcp_rn(t); }); }
+// 1/x: the hardware reciprocal approximation (max. 1 ulp) refined by one Newton step r += r (1 - x r),
+// the Newton step in V arithmetic (x is a density of order 1, or 2^15 in FP16S storage units)
+template<class V> __device__ __forceinline__ V v_rcp(const V x) {
+	const V r = v_map(x, [](const float t) { float y; asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(t)); return y; });
+	return v_fma(r, v_fma(v_neg(x), r, v_set<V>(1.0f)), r);
+}
 
 // signed sum of v_d over the non-zero components of c_I (any order: fast mode); starts from the
 // first non-zero term, since adding to 0 cannot be folded away under IEEE rules
@@ -209,12 +202,21 @@ template<int Q, bool TRT, bool VF, int ST, int EMODE, class V, class M> __device
 			if constexpr(EMODE==2) f[0] = v_pick(g0, v_mul(w0, X), is_e); else f[0] = g0;
 		}
 	}
+	// w R, w R / 2 and w (R-K) once per weight class (straight, edge, corner directions)
+	constexpr int NC = Q==27 ? 3 : 2;
+	V rwc[NC], hrc[NC], wmc[NC];
+	#pragma unroll
+	for(int c=0; c<NC; c++) {
+		const float wc = vs_w<Q>(c==0 ? 1 : c==1 ? 7 : 19);
+		rwc[c] = v_mul(v_set<V>(wc), R); hrc[c] = v_mul(v_set<V>(0.5f*wc), R); wmc[c] = v_mul(v_set<V>(wc), Rm1);
+	}
 	Unroll<1, Q, 2>::run([&](auto ic) {
 		constexpr int i = decltype(ic)::value;
+		constexpr int c = (vs_c(0, i)!=0)+(vs_c(1, i)!=0)+(vs_c(2, i)!=0)-1;
 		const float wi = vs_w<Q>(i);
-		const V rw = v_mul(v_set<V>(wi), R);
+		const V rw = rwc[c];
 		const V uk = csum_v<i>(ux3, uy3, uz3);
-		const V base = v_fma(v_mul(v_set<V>(0.5f*wi), R), v_fma(uk, uk, c3), v_mul(v_set<V>(wi), Rm1));
+		const V base = v_fma(hrc[c], v_fma(uk, uk, c3), wmc[c]);
 		const V ea = v_fma(rw, uk, base), eb = v_fma(v_neg(rw), uk, base);
 		if constexpr(EMODE==1) { f[i] = ea; f[i+1] = eb; }
 		else {

@@ -160,7 +160,7 @@ inline dim3 pair_grid(const GridDesc& g) { return dim3((g.NxNy/2u+BLOCK-1u)/BLOC
 inline bool pairs_supported(const GridDesc& g) { return g.Nx%2u==0u && g.N<=0xFFFFFFFFull; }
 
 #ifndef FX3D_PAIRS_MIN_BLOCKS
-#define FX3D_PAIRS_MIN_BLOCKS 3 // resident 256-thread blocks per SM the register budget is sized for (80 registers)
+#define FX3D_PAIRS_MIN_BLOCKS 2 // resident 256-thread blocks per SM the register budget is sized for
 #endif
 template<int Q, int ST, bool TRT, int EXT> __global__ void __launch_bounds__(BLOCK, FX3D_PAIRS_MIN_BLOCKS) k_stream_collide_pairs(const StepArgs a) {
 	typedef typename Codec<ST>::T T;
@@ -575,13 +575,14 @@ template<int ST, int Q, bool TRT> inline cudaError_t sc_ext(const int ext, const
 	}
 }
 template<int ST> cudaError_t launch_stream_collide_t(const Variant& v, const StepArgs& a, const int path, cudaStream_t s) {
-	// automatic choice (measured on 512x256x256): for fast arithmetic in place the two-cell kernel,
-	// with per-thread prefetch for 16-bit storage (FP32 moves enough bytes per access without it);
-	// otherwise one thread per cell in place, and the row-staged kernel for steps into another array
+	// automatic choice (measured on 512x256x256): for fast arithmetic in place with 16-bit storage the
+	// two-cell kernel with per-thread prefetch; otherwise one thread per cell in place (FP32 moves
+	// enough bytes per access to reach about 90% of the bandwidth that way), and the row-staged kernel
+	// for steps into another array
 	const bool rows_ok = row_plan(v.q, ST, a.g.Nx, a.g.Ny, a.g.Nz).stages!=0u;
 	const bool pairs_ok = v.fast && pairs_supported(a.g) && a.fi_dst==a.fi;
 	int kind = path;
-	if(path==PATH_AUTO) kind = pairs_ok ? (ST==ST_FP32 ? PATH_PAIRS : PATH_PIPE) : a.fi_dst!=a.fi ? PATH_ROWS : PATH_CELLS;
+	if(path==PATH_AUTO) kind = pairs_ok && ST!=ST_FP32 ? PATH_PIPE : a.fi_dst!=a.fi ? PATH_ROWS : PATH_CELLS;
 	if((kind==PATH_ROWS && !rows_ok) || ((kind==PATH_PAIRS||kind==PATH_PIPE) && !pairs_ok)) return cudaErrorInvalidConfiguration;
 	if(v.q==19) return v.trt ? sc_ext<ST, 19, true>(v.ext, a, kind, v.fast, s) : sc_ext<ST, 19, false>(v.ext, a, kind, v.fast, s);
 	if(v.q==27) return v.trt ? sc_ext<ST, 27, true>(v.ext, a, kind, v.fast, s) : sc_ext<ST, 27, false>(v.ext, a, kind, v.fast, s);
