@@ -51,55 +51,96 @@ template<int Q, bool VF> __device__ __forceinline__ void adj_forward(const float
 	s.c3 = -3.0f*fmaf(s.u[0], s.u[0], fmaf(s.u[1], s.u[1], s.u[2]*s.u[2]));
 }
 
-// gbar = (dh/dg)^T hbar + ke_weight * d(1/2 rho |u|^2)/dg; Fbar += (dh/dFt)^T hbar (+ objective part)
-template<int Q, bool TRT, bool VF> __device__ __forceinline__ void adj_cell(const CellState<Q>& s, const bool is_e, const float* hbar, const float ke_weight,
-                                                                         const StepArgs& a, float* gbar, float* Fbar) {
-	float feqbar[Q], Gbar[Q];
-	if(is_e) {
-		#pragma unroll
-		for(int i=0; i<Q; i++) { gbar[i] = 0.0f; feqbar[i] = hbar[i]; Gbar[i] = 0.0f; }
-	} else if constexpr(!TRT) {
-		#pragma unroll
-		for(int i=0; i<Q; i++) { gbar[i] = a.omw*hbar[i]; feqbar[i] = a.w*hbar[i]; Gbar[i] = a.c_tau*hbar[i]; }
-	} else {
-		gbar[0] = fmaf(-2.0f*a.hp, hbar[0], hbar[0]); feqbar[0] = 2.0f*a.hp*hbar[0]; Gbar[0] = 2.0f*a.c_taup*hbar[0];
-		#pragma unroll
-		for(int i=1; i<Q; i+=2) {
-			const float x = hbar[i], y = hbar[i+1], sp = x+y, sm = x-y;
-			const float di = fmaf(a.hp, sp, a.hm*sm), dj = fmaf(a.hp, sp, -a.hm*sm);
-			gbar[i] = x-di; gbar[i+1] = y-dj; feqbar[i] = di; feqbar[i+1] = dj;
-			Gbar[i] = fmaf(a.c_taup, sp, a.c_taum*sm); Gbar[i+1] = fmaf(a.c_taup, sp, -a.c_taum*sm);
-		}
+// Adjoint of the collision for one direction pair (i, i+1) (or the rest direction): from hbar the
+// collision part of gbar (gi, gj), the equilibrium adjoint (fi, fj) and the Guo-term adjoint (Gi, Gj)
+__device__ __forceinline__ void coll_bar_rest(const float h, const bool is_e, const bool trt, const StepArgs& a, float& gb, float& fb, float& Gb) {
+	if(is_e) { gb = 0.0f; fb = h; Gb = 0.0f; }
+	else if(!trt) { gb = a.omw*h; fb = a.w*h; Gb = a.c_tau*h; }
+	else { gb = fmaf(-2.0f*a.hp, h, h); fb = 2.0f*a.hp*h; Gb = 2.0f*a.c_taup*h; }
+}
+__device__ __forceinline__ void coll_bar_pair(const float x, const float y, const bool is_e, const bool trt, const StepArgs& a,
+                                              float& gi, float& gj, float& fi, float& fj, float& Gi, float& Gj) {
+	if(is_e) { gi = 0.0f; gj = 0.0f; fi = x; fj = y; Gi = 0.0f; Gj = 0.0f; }
+	else if(!trt) { gi = a.omw*x; gj = a.omw*y; fi = a.w*x; fj = a.w*y; Gi = a.c_tau*x; Gj = a.c_tau*y; }
+	else {
+		const float sp = x+y, sm = x-y;
+		const float di = fmaf(a.hp, sp, a.hm*sm), dj = fmaf(a.hp, sp, -a.hm*sm);
+		gi = x-di; gj = y-dj; fi = di; fj = dj;
+		Gi = fmaf(a.c_taup, sp, a.c_taum*sm); Gj = fmaf(a.c_taup, sp, -a.c_taum*sm);
 	}
-	// equilibrium
-	float rhobar = 0.0f, ubar[3] = {0.0f, 0.0f, 0.0f};
-	Unroll<0, Q, 1>::run([&](auto ic) {
+}
+// Moments over the directions of a per-direction weight v_i: m0 = sum v, m1_d = sum v c_d,
+// m2 = sum v c c^T (xx, yy, zz, xy, xz, yz). The equilibrium and Guo-term adjoints of all directions
+// depend on their per-direction factors only through these moments (below), so a direction costs a
+// few signed additions instead of a pass through the full chain rule.
+struct DirMoments {
+	float m0 = 0.0f, m1[3] = {0.0f, 0.0f, 0.0f}, m2[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+};
+template<int I> __device__ __forceinline__ void acc_moments(DirMoments& M, const float v) {
+	constexpr int cx = vs_c(0, I), cy = vs_c(1, I), cz = vs_c(2, I);
+	M.m0 += v;
+	if constexpr(cx!=0) { M.m1[0] += cx>0 ? v : -v; M.m2[0] += v; }
+	if constexpr(cy!=0) { M.m1[1] += cy>0 ? v : -v; M.m2[1] += v; }
+	if constexpr(cz!=0) { M.m1[2] += cz>0 ? v : -v; M.m2[2] += v; }
+	if constexpr(cx!=0 && cy!=0) M.m2[3] += cx*cy>0 ? v : -v;
+	if constexpr(cx!=0 && cz!=0) M.m2[4] += cx*cz>0 ? v : -v;
+	if constexpr(cy!=0 && cz!=0) M.m2[5] += cy*cz>0 ? v : -v;
+}
+__device__ __forceinline__ void m2_times(const DirMoments& M, const float* x, float* y) { // y = m2 x
+	y[0] = fmaf(M.m2[0], x[0], fmaf(M.m2[3], x[1], M.m2[4]*x[2]));
+	y[1] = fmaf(M.m2[3], x[0], fmaf(M.m2[1], x[1], M.m2[5]*x[2]));
+	y[2] = fmaf(M.m2[4], x[0], fmaf(M.m2[5], x[1], M.m2[2]*x[2]));
+}
+// With fb_i = w_i feqbar_i (feq_i = w_i (rho (0.5 (uk^2 + c3) + uk) + rho - 1), uk = 3 c_i.u, c3 = -3 |u|^2):
+//   rhobar += sum fb (0.5 (uk^2 + c3) + uk + 1) = 4.5 u.M2 u + (0.5 c3 + 1) M0 + 3 M1.u
+//   ubar_d += rho sum fb (3 c_d (uk + 1) - 3 u_d) = rho (9 (M2 u)_d + 3 M1_d - 3 u_d M0)
+// and with gb_i = 9 w_i Gbar_i (G_i = 9 w_i ((c_i.Ft)(c_i.u + 1/3) - u.Ft/3)):
+//   ubar_d  += sum gb (c.Ft c_d - Ft_d/3)      = (S2 Ft)_d - Ft_d S0/3
+//   Ftbar_d += sum gb (c_d (c.u + 1/3) - u_d/3) = (S2 u)_d + S1_d/3 - u_d S0/3
+template<int Q> __device__ __forceinline__ void eq_moments_bar(const CellState<Q>& s, const DirMoments& M, float& rhobar, float* ubar) {
+	float M2u[3];
+	m2_times(M, s.u, M2u);
+	const float uM2u = fmaf(s.u[0], M2u[0], fmaf(s.u[1], M2u[1], s.u[2]*M2u[2]));
+	const float M1u = fmaf(M.m1[0], s.u[0], fmaf(M.m1[1], s.u[1], M.m1[2]*s.u[2]));
+	rhobar += fmaf(4.5f, uM2u, fmaf(fmaf(0.5f, s.c3, 1.0f), M.m0, 3.0f*M1u));
+	#pragma unroll
+	for(int d=0; d<3; d++) ubar[d] = fmaf(s.rho, fmaf(9.0f, M2u[d], fmaf(3.0f, M.m1[d], -3.0f*s.u[d]*M.m0)), ubar[d]);
+}
+template<int Q> __device__ __forceinline__ void guo_moments_bar(const CellState<Q>& s, const DirMoments& S, float* ubar, float* Ftbar) {
+	float S2F[3], S2u[3];
+	m2_times(S, s.Ft, S2F);
+	m2_times(S, s.u, S2u);
+	#pragma unroll
+	for(int d=0; d<3; d++) {
+		ubar[d] += fmaf(-s.Ft[d]*THIRD, S.m0, S2F[d]);
+		Ftbar[d] += fmaf(-s.u[d]*THIRD, S.m0, fmaf(S.m1[d], THIRD, S2u[d]));
+	}
+}
+
+// (dh/dg)^T hbar + ke_weight * d(1/2 rho |u|^2)/dg in two passes over the direction pairs, so that
+// only hbar stays live: pass 1 accumulates rhobar, ubar and Ftbar (Fbar += Ftbar); afterwards
+// gbar_i = (collision part of direction i) + rhobar + c_i.mbar, recomputed per direction and handed
+// to put(integral_constant<int, i>, gbar_i)
+template<int Q, bool TRT, bool VF, class PUT> __device__ __forceinline__ void adj_cell(const CellState<Q>& s, const bool is_e, const float* hbar,
+                                                                                     const float ke_weight, const StepArgs& a, float* Fbar, PUT&& put) {
+	float rhobar = 0.0f, ubar[3] = {0.0f, 0.0f, 0.0f}, Ftbar[3] = {0.0f, 0.0f, 0.0f};
+	DirMoments M, S; // moments of w_i feqbar_i and of 9 w_i Gbar_i
+	{
+		float gb, fb, Gb;
+		coll_bar_rest(hbar[0], is_e, TRT, a, gb, fb, Gb);
+		acc_moments<0>(M, vs_w<Q>(0)*fb);
+		if constexpr(VF) acc_moments<0>(S, (9.0f*vs_w<Q>(0))*Gb);
+	}
+	Unroll<1, Q, 2>::run([&](auto ic) {
 		constexpr int i = decltype(ic)::value;
-		const float wi = vs_w<Q>(i);
-		const float uk = 3.0f*(vs_c(0, i)*s.u[0]+vs_c(1, i)*s.u[1]+vs_c(2, i)*s.u[2]);
-		const float fb = feqbar[i]*wi;
-		rhobar = fmaf(fb, fmaf(0.5f, fmaf(uk, uk, s.c3), uk+1.0f), rhobar);
-		const float fbr = fb*s.rho;
-		#pragma unroll
-		for(int d=0; d<3; d++) {
-			const int cd = d==0 ? vs_c(0, i) : d==1 ? vs_c(1, i) : vs_c(2, i);
-			ubar[d] = fmaf(fbr, 3.0f*(cd*(uk+1.0f))-3.0f*s.u[d], ubar[d]);
-		}
+		float gi, gj, fi, fj, Gi, Gj;
+		coll_bar_pair(hbar[i], hbar[i+1], is_e, TRT, a, gi, gj, fi, fj, Gi, Gj);
+		const float wi = vs_w<Q>(i); // w_{i+1} = w_i
+		acc_moments<i>(M, wi*fi); acc_moments<i+1>(M, wi*fj);
+		if constexpr(VF) { acc_moments<i>(S, (9.0f*wi)*Gi); acc_moments<i+1>(S, (9.0f*wi)*Gj); }
 	});
-	float Ftbar[3] = {0.0f, 0.0f, 0.0f};
-	if constexpr(VF) {
-		if(!is_e) {
-			Unroll<0, Q, 1>::run([&](auto ic) {
-				constexpr int i = decltype(ic)::value;
-				const float wi9 = 9.0f*vs_w<Q>(i)*Gbar[i];
-				constexpr int cx = vs_c(0, i), cy = vs_c(1, i), cz = vs_c(2, i);
-				const float cf = cx*s.Ft[0]+cy*s.Ft[1]+cz*s.Ft[2], cu = cx*s.u[0]+cy*s.u[1]+cz*s.u[2];
-				ubar[0] = fmaf(wi9, cf*cx-s.Ft[0]*THIRD, ubar[0]); Ftbar[0] = fmaf(wi9, cx*(cu+THIRD)-s.u[0]*THIRD, Ftbar[0]);
-				ubar[1] = fmaf(wi9, cf*cy-s.Ft[1]*THIRD, ubar[1]); Ftbar[1] = fmaf(wi9, cy*(cu+THIRD)-s.u[1]*THIRD, Ftbar[1]);
-				ubar[2] = fmaf(wi9, cf*cz-s.Ft[2]*THIRD, ubar[2]); Ftbar[2] = fmaf(wi9, cz*(cu+THIRD)-s.u[2]*THIRD, Ftbar[2]);
-			});
-		}
-	}
+	eq_moments_bar<Q>(s, M, rhobar, ubar);
+	if constexpr(VF) { if(!is_e) guo_moments_bar<Q>(s, S, ubar, Ftbar); }
 	if(ke_weight!=0.0f && !is_e) {
 		rhobar = fmaf(ke_weight*0.5f, fmaf(s.u[0], s.u[0], fmaf(s.u[1], s.u[1], s.u[2]*s.u[2])), rhobar);
 		#pragma unroll
@@ -112,58 +153,63 @@ template<int Q, bool TRT, bool VF> __device__ __forceinline__ void adj_cell(cons
 		u0bar[d] = vbar;
 		if constexpr(VF) { Ftbar[d] = fmaf(vbar, s.rho2, Ftbar[d]); rho2bar = fmaf(vbar, s.Ft[d], rho2bar); }
 	}
+	float mbar[3] = {0.0f, 0.0f, 0.0f};
 	if(!is_e) {
 		const float inv = 1.0f/s.rho;
 		rhobar = fmaf(rho2bar, -2.0f*s.rho2*s.rho2, rhobar); // d(0.5/rho)/drho = -0.5/rho^2 = -2 rho2^2
-		float mbar[3];
 		#pragma unroll
 		for(int d=0; d<3; d++) { mbar[d] = u0bar[d]*inv; rhobar = fmaf(-u0bar[d]*inv, s.u0[d], rhobar); }
-		Unroll<0, Q, 1>::run([&](auto ic) {
-			constexpr int i = decltype(ic)::value;
-			float gb = gbar[i]+rhobar;
-			if constexpr(vs_c(0, i)!=0) gb += vs_c(0, i)>0 ? mbar[0] : -mbar[0];
-			if constexpr(vs_c(1, i)!=0) gb += vs_c(1, i)>0 ? mbar[1] : -mbar[1];
-			if constexpr(vs_c(2, i)!=0) gb += vs_c(2, i)>0 ? mbar[2] : -mbar[2];
-			gbar[i] = gb;
-		});
+	} else {
+		rhobar = 0.0f; // TYPE_E cells pass nothing back to g
 	}
+	auto finish = [&](const int cx, const int cy, const int cz, const float gcoll) {
+		float gb = gcoll+rhobar;
+		if(cx!=0) gb += cx>0 ? mbar[0] : -mbar[0];
+		if(cy!=0) gb += cy>0 ? mbar[1] : -mbar[1];
+		if(cz!=0) gb += cz>0 ? mbar[2] : -mbar[2];
+		return gb;
+	};
+	{
+		float gb, fb, Gb;
+		coll_bar_rest(hbar[0], is_e, TRT, a, gb, fb, Gb);
+		put(std::integral_constant<int, 0>(), finish(0, 0, 0, gb));
+	}
+	Unroll<1, Q, 2>::run([&](auto ic) {
+		constexpr int i = decltype(ic)::value;
+		float gi, gj, fi, fj, Gi, Gj;
+		coll_bar_pair(hbar[i], hbar[i+1], is_e, TRT, a, gi, gj, fi, fj, Gi, Gj);
+		put(std::integral_constant<int, i>(), finish(vs_c(0, i), vs_c(1, i), vs_c(2, i), gi));
+		put(std::integral_constant<int, i+1>(), finish(vs_c(0, i+1), vs_c(1, i+1), vs_c(2, i+1), gj));
+	});
 	#pragma unroll
 	for(int d=0; d<3; d++) Fbar[d] += Ftbar[d];
 }
 
-// load / store positions of the slot set of cell n at the parity of step t:
-// load reads g_0 from (n,0), g_i from A_i, g_{i+1} from B_i; store writes h_i to B_i, h_{i+1} to A_i
-template<int Q> struct SlotSet {
-	uint64_t A[Q], B[Q];
-	__device__ __forceinline__ SlotSet(const uint64_t N, const uint64_t n, const Nbr& nb, const bool odd) {
-		const uint64_t e = odd ? 0ull : N;
-		Unroll<1, Q, 2>::run([&](auto ic) {
-			constexpr int i = decltype(ic)::value;
-			A[i] = (uint64_t)i*N+e+n;
-			B[i] = (uint64_t)(i+1)*N-e+nb.template j<i>();
-		});
-	}
-};
-
-// OBJ_ONLY: add only the objective's dj/dg (lambda += ..., hbar = 0): the final state of the window
-template<int Q, int ST, bool TRT, int EXT, bool OBJ_ONLY> __global__ void __launch_bounds__(BLOCK) k_adjoint_step(const StepArgs a, const AdjArgs j) {
+// OBJ_ONLY: add only the objective's dj/dg (lambda += ..., hbar = 0): the final state of the window.
+// Slot positions of cell n at the step's parity (32-bit cell indices, N < 2^32): g_0 at n, g_i at
+// A_i = i N + e + n, g_{i+1} at B_i = (i+1) N - e + j_i (e = 0 at odd t, N at even t); the forward
+// store wrote h_i to B_i and h_{i+1} to A_i, so hbar is read there and gbar written to the load positions.
+template<int Q, int ST, bool TRT, int EXT, bool OBJ_ONLY> __global__ void __launch_bounds__(BLOCK, 3) k_adjoint_step(const StepArgs a, const AdjArgs j) {
 	typedef typename Codec<ST>::T T;
 	constexpr bool VF = (EXT&EXT_VF)!=0, FF = (EXT&EXT_FF)!=0, EQ = (EXT&EXT_EQ)!=0;
 	const Grid& g = grid_of(a.g);
 	CellPos c;
 	if(!cell_of_thread(g, c)) return;
-	const uint64_t n = c.n, N = g.N;
+	const uint32_t n = (uint32_t)c.n;
+	const uint64_t N = g.N, e = (a.t&1ull)!=0ull ? 0ull : N;
+	const bool odd = (a.t&1ull)!=0ull;
 	const uint8_t fl = a.flags[n];
 	const uint8_t bo = fl&TYPE_BO;
-	const bool odd = (a.t&1ull)!=0ull;
-	const Nbr nb(g, c.x, c.y, c.z);
+	const Steps32 st(g, c.x, c.y, c.z, n);
+	float* const L = j.lambda;
+	auto A = [&](const int i) -> float& { return (L+((uint64_t)i*N+e))[n]; };
+	auto B = [&](auto ic) -> float& { constexpr int i = decltype(ic)::value; return (L+((uint64_t)(i+1)*N-e))[st.template j<i>()]; };
 	if(bo==TYPE_S||(fl&TYPE_SU)==TYPE_G) { // identity map; the drag objective lives on these cells
 		if(j.obj_kind==OBJ_DRAG_X && j.obj_weight!=0.0f && fl==(uint8_t)j.marker) {
-			const SlotSet<Q> ss(N, n, nb, odd);
 			const float w2 = 2.0f*j.obj_weight;
 			Unroll<1, Q, 2>::run([&](auto ic) {
 				constexpr int i = decltype(ic)::value, cx = vs_c(0, i);
-				if constexpr(cx!=0) { j.lambda[ss.A[i]] += cx*w2; j.lambda[ss.B[i]] -= cx*w2; } // g_i at A_i (c_i), g_{i+1} at B_i (-c_i)
+				if constexpr(cx!=0) { A(i) += cx*w2; B(ic) -= cx*w2; } // g_i at A_i (c_i), g_{i+1} at B_i (-c_i)
 			});
 		}
 		return;
@@ -171,30 +217,33 @@ template<int Q, int ST, bool TRT, int EXT, bool OBJ_ONLY> __global__ void __laun
 	const bool is_e = EQ && bo==TYPE_E;
 	const bool ke = j.obj_kind==OBJ_KE_PLANE && j.obj_weight!=0.0f && c.x==j.plane_x && !is_e;
 	if(OBJ_ONLY && !ke) return;
-	const SlotSet<Q> ss(N, n, nb, odd);
-	float gv[Q], hbar[Q], gbar[Q];
-	load_f<Q, ST>((const T*)j.state, N, n, nb, odd, gv);
+	float hbar[Q];
 	if constexpr(OBJ_ONLY) {
 		#pragma unroll
 		for(int i=0; i<Q; i++) hbar[i] = 0.0f;
 	} else {
-		hbar[0] = j.lambda[n];
-		Unroll<1, Q, 2>::run([&](auto ic) { constexpr int i = decltype(ic)::value; hbar[i] = j.lambda[ss.B[i]]; hbar[i+1] = j.lambda[ss.A[i]]; });
+		hbar[0] = L[n];
+		Unroll<1, Q, 2>::run([&](auto ic) { constexpr int i = decltype(ic)::value; hbar[i] = B(ic); hbar[i+1] = A(i); });
 	}
-	float Ft[3] = {a.fx, a.fy, a.fz};
-	if constexpr(FF) { Ft[0] += a.F[n]; Ft[1] += a.F[N+n]; Ft[2] += a.F[2ull*N+n]; }
-	const float up[3] = {is_e ? a.u[n] : 0.0f, is_e ? a.u[N+n] : 0.0f, is_e ? a.u[2ull*N+n] : 0.0f};
 	CellState<Q> s;
-	adj_forward<Q, VF>(gv, is_e, is_e ? a.rho[n] : 1.0f, up, Ft, s);
-	float Fbar[3] = {0.0f, 0.0f, 0.0f};
-	adj_cell<Q, TRT, VF>(s, is_e, hbar, ke ? j.obj_weight : 0.0f, a, gbar, Fbar);
-	if constexpr(OBJ_ONLY) {
-		j.lambda[n] += gbar[0];
-		Unroll<1, Q, 2>::run([&](auto ic) { constexpr int i = decltype(ic)::value; j.lambda[ss.A[i]] += gbar[i]; j.lambda[ss.B[i]] += gbar[i+1]; });
-	} else {
-		j.lambda[n] = gbar[0];
-		Unroll<1, Q, 2>::run([&](auto ic) { constexpr int i = decltype(ic)::value; j.lambda[ss.A[i]] = gbar[i]; j.lambda[ss.B[i]] = gbar[i+1]; });
+	{
+		float gv[Q];
+		load_f32<Q, Codec<ST>>((const T*)j.state, N, st, odd, gv);
+		float Ft[3] = {a.fx, a.fy, a.fz};
+		if constexpr(FF) { Ft[0] += a.F[n]; Ft[1] += a.F[N+n]; Ft[2] += a.F[2ull*N+n]; }
+		const float up[3] = {is_e ? a.u[n] : 0.0f, is_e ? a.u[N+n] : 0.0f, is_e ? a.u[2ull*N+n] : 0.0f};
+		adj_forward<Q, VF>(gv, is_e, is_e ? a.rho[n] : 1.0f, up, Ft, s);
 	}
+	float Fbar[3] = {0.0f, 0.0f, 0.0f};
+	// gbar of direction k goes to the load position of g_k: n (k = 0), A_i (k = i odd), B_i (k = i+1)
+	adj_cell<Q, TRT, VF>(s, is_e, hbar, ke ? j.obj_weight : 0.0f, a, Fbar, [&](auto kc, const float v) {
+		constexpr int k = decltype(kc)::value;
+		float* p;
+		if constexpr(k==0) p = &L[n];
+		else if constexpr((k&1)!=0) p = &A(k);
+		else p = &B(std::integral_constant<int, k-1>());
+		if constexpr(OBJ_ONLY) *p += v; else *p = v;
+	});
 	if constexpr(FF) { j.grad[n] += Fbar[0]; j.grad[N+n] += Fbar[1]; j.grad[2ull*N+n] += Fbar[2]; }
 }
 

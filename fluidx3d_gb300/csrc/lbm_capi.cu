@@ -299,7 +299,7 @@ int lbm_domain_create(const lbm_config* c, lbm_domain** out) {
 	d->g.nx_inv = c->Nx==1u ? 0ull : (~0ull)/c->Nx+1ull; // ceil(2^64/Nx)
 	d->w = lbm_relaxation_rate(c->nu);
 	d->rates = make_rates(d->w);
-	// stream_collide implementation: FX3D_STREAM_COLLIDE_PATH=cells|rows|pairs|pipe forces one (diagnostics
+	// stream_collide implementation: FX3D_STREAM_COLLIDE_PATH=cells|rows|pairs|pipe|rowpairs forces one (diagnostics
 	// and tests); the default takes the two-cell packed kernel with per-thread prefetch for fast
 	// arithmetic on 16-bit storage where the lattice allows it (even Nx, fewer than 2^32 cells), else
 	// one thread per cell
@@ -308,6 +308,7 @@ int lbm_domain_create(const lbm_config* c, lbm_domain** out) {
 		else if(!std::strcmp(p, "rows")) d->path = PATH_ROWS;
 		else if(!std::strcmp(p, "pairs")) d->path = PATH_PAIRS;
 		else if(!std::strcmp(p, "pipe")) d->path = PATH_PIPE;
+		else if(!std::strcmp(p, "rowpairs")) d->path = PATH_ROWPAIRS;
 	}
 
 	cudaError_t e = cudaStreamCreateWithFlags(&d->own_stream, cudaStreamNonBlocking);
@@ -561,18 +562,22 @@ struct DeviceBuffer { // freed on scope exit
 	~DeviceBuffer() { if(p) cudaFree(p); }
 };
 
-// f^{k+1} = step(f^k) from src into dst (row-staged kernel out of place; otherwise copy, then in place)
+// f^{k+1} = step(f^k) from src into dst: one thread per cell steps out of place (the row-staged
+// kernel when that path is forced); the two-cell kernels step in place only, so with one of those
+// forced the state is copied first
 int step_out_of_place(lbm_domain* d, const void* src, void* dst, const uint64_t t) {
 	StepArgs a = d->args();
 	a.t = t;
-	const bool rows = (d->path==PATH_AUTO||d->path==PATH_ROWS) && row_plan(d->v.q, d->v.storage, d->g.Nx, d->g.Ny, d->g.Nz).stages!=0u;
-	if(rows) { a.fi = const_cast<void*>(src); a.fi_dst = dst; }
-	else {
+	const bool rows_ok = row_plan(d->v.q, d->v.storage, d->g.Nx, d->g.Ny, d->g.Nz).stages!=0u;
+	int path = d->path==PATH_ROWS && rows_ok ? PATH_ROWS : PATH_CELLS;
+	if(d->path==PATH_PAIRS||d->path==PATH_PIPE) {
 		FX3D_CUDA(cudaMemcpyAsync(dst, src, d->field_bytes(LBM_FIELD_FI), cudaMemcpyDeviceToDevice, d->stream), "cudaMemcpyAsync(state)");
 		a.fi = dst; a.fi_dst = dst;
+		path = d->path;
+	} else {
+		a.fi = const_cast<void*>(src); a.fi_dst = dst;
 	}
 	cudaError_t e;
-	const int path = rows ? PATH_ROWS : (d->path==PATH_PAIRS||d->path==PATH_PIPE) ? d->path : PATH_CELLS;
 	switch(d->v.storage) {
 		case ST_FP32: e = launch_stream_collide_fp32(d->v, a, path, d->stream); break;
 		case ST_FP16S: e = launch_stream_collide_fp16s(d->v, a, path, d->stream); break;
@@ -595,6 +600,7 @@ extern "C" int lbm_run_adjoint(lbm_domain* d, const lbm_adjoint_config* cfg, dou
 	if(!cfg) return fail(LBM_ERR_INVALID_ARGUMENT, "lbm_run_adjoint: NULL config");
 	if(!d->initialized) return fail(LBM_ERR_NOT_INITIALIZED, "lbm_run_adjoint: call lbm_initialize first");
 	if(!adjoint_supported(d->v) || !d->F) return fail(LBM_ERR_UNSUPPORTED, "lbm_run_adjoint needs LBM_EXT_VOLUME_FORCE and LBM_EXT_FORCE_FIELD (F is the design variable)");
+	if(d->g.N>0xFFFFFFFFull) return fail(LBM_ERR_UNSUPPORTED, "lbm_run_adjoint needs fewer than 2^32 cells (its kernels use 32-bit cell indices)");
 	if(cfg->steps==0ull||cfg->checkpoint_interval==0ull) return fail(LBM_ERR_INVALID_ARGUMENT, "lbm_run_adjoint: steps and checkpoint_interval must be >= 1");
 	if(cfg->objective!=LBM_OBJECTIVE_KINETIC_ENERGY_PLANE_X && cfg->objective!=LBM_OBJECTIVE_DRAG_X) return fail(LBM_ERR_INVALID_ARGUMENT, "lbm_run_adjoint: unknown objective %u", cfg->objective);
 	if(cfg->objective==LBM_OBJECTIVE_KINETIC_ENERGY_PLANE_X && cfg->plane_x>=d->g.Nx) return fail(LBM_ERR_INVALID_ARGUMENT, "lbm_run_adjoint: plane_x outside the lattice");

@@ -68,7 +68,8 @@ __device__ __forceinline__ float v_neg(const float a) { return -a; }
 __device__ __forceinline__ float2 v_add(const float2 a, const float2 b) { return __fadd2_rn(a, b); }
 __device__ __forceinline__ float2 v_mul(const float2 a, const float2 b) { return __fmul2_rn(a, b); }
 __device__ __forceinline__ float2 v_neg(const float2 a) { return make_float2(-a.x, -a.y); }
-__device__ __forceinline__ float2 v_sub(const float2 a, const float2 b) { return v_add(a, v_neg(b)); } // a-b == a+(-b) in IEEE
+// a-b as fma(b, -1, a): the product is exact, so this is a-b rounded once, with no separate negation
+__device__ __forceinline__ float2 v_sub(const float2 a, const float2 b) { return __ffma2_rn(b, make_float2(-1.0f, -1.0f), a); }
 __device__ __forceinline__ float2 v_fma(const float2 a, const float2 b, const float2 c) { return __ffma2_rn(a, b, c); }
 template<class V> __device__ __forceinline__ V v_set(const float s);
 template<> __device__ __forceinline__ float v_set<float>(const float s) { return s; }
@@ -92,18 +93,29 @@ template<class V> __device__ __forceinline__ V v_rcp(const V x) {
 	return v_fma(r, v_fma(v_neg(x), r, v_set<V>(1.0f)), r);
 }
 
-// signed sum of v_d over the non-zero components of c_I (any order: fast mode); starts from the
-// first non-zero term, since adding to 0 cannot be folded away under IEEE rules
+// signed sum of v_d over the non-zero components of c_I (any order: fast mode): starts from the first
+// component with a positive sign and adds or subtracts the others in component order, so that no
+// negation is needed (every odd direction of D3Q19/D3Q27 has a positive component); adding to 0
+// cannot be folded away under IEEE rules, so no zero start either
+template<int I> __host__ __device__ constexpr int csum_first() { return vs_c(0, I)>0 ? 0 : vs_c(1, I)>0 ? 1 : vs_c(2, I)>0 ? 2 : -1; }
 template<int I, class V> __device__ __forceinline__ V csum_v(const V vx, const V vy, const V vz) {
-	constexpr int a = vs_c(0, I), b = vs_c(1, I), c = vs_c(2, I);
-	const V tx = a>0 ? vx : v_neg(vx), ty = b>0 ? vy : v_neg(vy), tz = c>0 ? vz : v_neg(vz);
-	if constexpr(a!=0 && b!=0 && c!=0) return v_add(v_add(tx, ty), tz);
-	else if constexpr(a!=0 && b!=0) return v_add(tx, ty);
-	else if constexpr(a!=0 && c!=0) return v_add(tx, tz);
-	else if constexpr(b!=0 && c!=0) return v_add(ty, tz);
-	else if constexpr(a!=0) return tx;
-	else if constexpr(b!=0) return ty;
-	else return tz;
+	const V v[3] = {vx, vy, vz};
+	if constexpr(csum_first<I>()<0) { // no positive component: -(sum of the magnitudes)
+		V s = v_set<V>(0.0f);
+		bool set = false;
+		Unroll<0, 3, 1>::run([&](auto dc) {
+			constexpr int d = decltype(dc)::value;
+			if constexpr(vs_c(d, I)!=0) { s = set ? v_add(s, v[d]) : v[d]; set = true; }
+		});
+		return v_neg(s);
+	} else {
+		V s = v[csum_first<I>()];
+		Unroll<0, 3, 1>::run([&](auto dc) {
+			constexpr int d = decltype(dc)::value;
+			if constexpr(d!=csum_first<I>() && vs_c(d, I)!=0) s = vs_c(d, I)>0 ? v_add(s, v[d]) : v_sub(s, v[d]);
+		});
+		return s;
+	}
 }
 
 // accumulate d with sign C into an accumulator that starts unset (no addition to 0)
@@ -151,7 +163,8 @@ template<int Q, int EXT, int ST, class V, class M> __device__ __forceinline__ vo
 		inv = v_rcp(R);
 		// u = m/R from the reciprocal plus one Newton correction (u += (m - u R)/R)
 		ux = v_mul(mx, inv); uy = v_mul(my, inv); uz = v_mul(mz, inv);
-		ux = v_fma(v_fma(v_neg(ux), R, mx), inv, ux); uy = v_fma(v_fma(v_neg(uy), R, my), inv, uy); uz = v_fma(v_fma(v_neg(uz), R, mz), inv, uz);
+		const V nR = v_neg(R); // fma(u, -R, m) == fma(-u, R, m)
+		ux = v_fma(v_fma(ux, nR, mx), inv, ux); uy = v_fma(v_fma(uy, nR, my), inv, uy); uz = v_fma(v_fma(uz, nR, mz), inv, uz);
 	};
 	if constexpr(std::is_same<V, float>::value) {
 		if(is_e) from_fields(R, Rm1, inv, ux, uy, uz);
@@ -204,11 +217,11 @@ template<int Q, bool TRT, bool VF, int ST, int EMODE, class V, class M> __device
 	}
 	// w R, w R / 2 and w (R-K) once per weight class (straight, edge, corner directions)
 	constexpr int NC = Q==27 ? 3 : 2;
-	V rwc[NC], hrc[NC], wmc[NC];
+	V rwc[NC], nrwc[NC], hrc[NC], wmc[NC];
 	#pragma unroll
 	for(int c=0; c<NC; c++) {
 		const float wc = vs_w<Q>(c==0 ? 1 : c==1 ? 7 : 19);
-		rwc[c] = v_mul(v_set<V>(wc), R); hrc[c] = v_mul(v_set<V>(0.5f*wc), R); wmc[c] = v_mul(v_set<V>(wc), Rm1);
+		rwc[c] = v_mul(v_set<V>(wc), R); nrwc[c] = v_mul(v_set<V>(-wc), R); hrc[c] = v_mul(v_set<V>(0.5f*wc), R); wmc[c] = v_mul(v_set<V>(wc), Rm1);
 	}
 	Unroll<1, Q, 2>::run([&](auto ic) {
 		constexpr int i = decltype(ic)::value;
@@ -217,7 +230,7 @@ template<int Q, bool TRT, bool VF, int ST, int EMODE, class V, class M> __device
 		const V rw = rwc[c];
 		const V uk = csum_v<i>(ux3, uy3, uz3);
 		const V base = v_fma(hrc[c], v_fma(uk, uk, c3), wmc[c]);
-		const V ea = v_fma(rw, uk, base), eb = v_fma(v_neg(rw), uk, base);
+		const V ea = v_fma(rw, uk, base), eb = v_fma(nrwc[c], uk, base);
 		if constexpr(EMODE==1) { f[i] = ea; f[i+1] = eb; }
 		else {
 			const V da = v_sub(ea, f[i]), db = v_sub(eb, f[i+1]);

@@ -147,8 +147,10 @@ def adjoint_setup(storage="fp32", Nx=128, Ny=64, Nz=64, sigma=1e-5, seed=4, coll
     return lbm
 
 
-def adjoint(steps=2000, window=(1800, 2000), plane_x=120, interval=100):
-    """dJ/dF, J = mean kinetic energy on plane x=120 over steps 1800-2000; adjoint/forward time ratio."""
+def adjoint(steps=2000, window=None, plane_x=120, interval=100):
+    """dJ/dF, J = mean kinetic energy on plane x=120 over steps 1800-2000 (the last tenth of the run);
+    adjoint/forward time ratio."""
+    window = window or (steps - steps // 10, steps)
     with adjoint_setup() as lbm:
         J, grad, st = lbm.run_adjoint(steps, "ke_plane", window=window, plane_x=plane_x, checkpoint_interval=interval)
     with adjoint_setup() as lbm:
@@ -160,8 +162,10 @@ def adjoint(steps=2000, window=(1800, 2000), plane_x=120, interval=100):
                 gradient_over_forward=total / t.ms), grad
 
 
-def adjoint_scale(steps=10000, window=(9000, 10000), interval=200, storage="fp16s"):
-    """dJ/dF on the sphere channel, J = x drag on the sphere averaged over steps 9000-10000, F = 0."""
+def adjoint_scale(steps=10000, window=None, interval=200, storage="fp16s"):
+    """dJ/dF on the sphere channel, J = x drag on the sphere averaged over steps 9000-10000 (the last
+    tenth of the run), F = 0."""
+    window = window or (steps - steps // 10, steps)
     with sphere_setup(storage, "trt", extensions=("eq", "ff", "vf")) as lbm:
         J, grad, st = lbm.run_adjoint(steps, "drag_x", window=window, marker=TYPE_S | TYPE_X, checkpoint_interval=interval)
     with sphere_setup(storage, "trt", extensions=("eq", "ff", "vf")) as lbm:

@@ -68,6 +68,7 @@ def lib() -> ctypes.CDLL:
             getattr(L, f"oracle_update_force_field_{s}").argtypes = [cfg, v, v, u64, v]
         L.oracle_object_sum.argtypes = [cfg, ctypes.c_int, v, v, u8, d, d, d, v]
         L.oracle_voxelize_mesh.argtypes = [cfg, u32, v, v, v, u64, u8, v, v, v, v]
+        L.oracle_voxelize_rays.argtypes = [cfg, u32, v, v, v, u64, u8, v, v, v, v, v, u64]
         L.oracle_unvoxelize_mesh.argtypes = [cfg, v, u8, f32, f32, f32, f32, f32, f32]
         L.oracle_fp16s_encode.argtypes = [f32]; L.oracle_fp16s_encode.restype = u16
         L.oracle_fp16s_decode.argtypes = [u16]; L.oracle_fp16s_decode.restype = f32
@@ -150,6 +151,23 @@ class Oracle:
 
     def unvoxelize_mesh(self, flag, x0, y0, z0, x1, y1, z1):
         self._chk(lib().oracle_unvoxelize_mesh(ctypes.byref(self.cfg), _p(self.flags), flag, x0, y0, z0, x1, y1, z1), "unvoxelize_mesh")
+
+
+def voxelize_rays(shape, flags, direction, flag, p0, p1, p2, bbu, rays, q=19, threads=None):
+    """The FP32 voxelizer restatement (src/kernel.cpp:2267-2357) on a subset of rays only, into a
+    flags array of the whole lattice (no DDFs or velocities: for a mesh without velocity over cells
+    that start without the mesh's flag). Ray index a as the kernel's: direction 0 a = y + z*Ny,
+    1 a = z + x*Nz, 2 a = x + y*Nx."""
+    Nx, Ny, Nz = (int(v) for v in shape)
+    assert flags.dtype == np.uint8 and flags.size == Nx * Ny * Nz
+    assert not np.any(np.asarray(bbu[7:16], np.float32)[3:] != 0.0), "mesh velocity needs DDFs and u"
+    cfg = OracleConfig(Nx, Ny, Nz, q, 0, STORAGE["fp32"], 0, threads or os.cpu_count() or 1, 1.0)
+    rays = np.ascontiguousarray(rays, dtype=np.uint64)
+    rc = lib().oracle_voxelize_rays(ctypes.byref(cfg), direction, None, None, _p(flags), 0, flag, _p(np.ascontiguousarray(p0, np.float32)),
+                                    _p(np.ascontiguousarray(p1, np.float32)), _p(np.ascontiguousarray(p2, np.float32)),
+                                    _p(np.ascontiguousarray(bbu, np.float32)), _p(rays), rays.size)
+    if rc != 0:
+        raise RuntimeError(f"oracle voxelize_rays failed ({rc})")
 
 
 def ref_variant_name(q, collision, storage, extensions=()) -> str:

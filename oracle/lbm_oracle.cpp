@@ -381,8 +381,9 @@ static inline f3 cross(const f3 a, const f3 b) { return {a.y*b.z-a.z*b.y, a.z*b.
 static inline float dot(const f3 a, const f3 b) { return a.x*b.x+a.y*b.y+a.z*b.z; }
 static inline int clampi(const int x, const int a, const int b) { return x<a ? a : x>b ? b : x; }
 
+// rays: the ray indices to cast (NULL: all A rays of the direction), nrays their count
 static int voxelize_impl(const OracleConfig* c, const u32 direction, void* fi, float* u, u8* flags, const u64 t, const u8 flag,
-                         const float* p0, const float* p1, const float* p2, const float* bbu) {
+                         const float* p0, const float* p1, const float* p2, const float* bbu, const u64* rays = nullptr, const u64 nrays = 0u) {
 	const Grid G(c); const u32 q = c->q;
 	const u32 Nx = G.Nx, Ny = G.Ny, Nz = G.Nz;
 	const u64 A = direction==0u ? (u64)Ny*Nz : direction==1u ? (u64)Nz*Nx : (u64)Nx*Ny;
@@ -394,7 +395,9 @@ static int voxelize_impl(const OracleConfig* c, const u32 direction, void* fi, f
 	const f3 offset = {0.5f*(float)(int)Nx-0.5f, 0.5f*(float)(int)Ny-0.5f, 0.5f*(float)(int)Nz-0.5f};
 	const f3 r_dir = {(float)(direction==0u), (float)(direction==1u), (float)(direction==2u)};
 	const bool set_u = ux*ux+uy*uy+uz*uz+rx*rx+ry*ry+rz*rz>0.0f;
-	parallel_cells(A, c->threads, [&](const u64 ai) {
+	parallel_cells(rays ? nrays : A, c->threads, [&](const u64 k) {
+		const u64 ai = rays ? rays[k] : k;
+		if(ai>=A) return;
 		const u32 a = (u32)ai;
 		u32 X, Y, Z;
 		if(direction==0u) { X = hmin; Y = a%Ny; Z = a/Ny; }
@@ -528,6 +531,11 @@ int oracle_object_sum(const OracleConfig* c, const int kind, const float* F, con
 int oracle_voxelize_mesh(const OracleConfig* c, const u32 direction, void* fi, float* u, u8* flags, const u64 t, const u8 flag,
                          const float* p0, const float* p1, const float* p2, const float* bbu) {
 	return valid(c) && direction<3u ? voxelize_impl(c, direction, fi, u, flags, t, flag, p0, p1, p2, bbu) : -1;
+}
+// the same for a subset of rays (ray index a as in voxelize_mesh: direction 0 a = Y + Z*Ny, 1 a = Z + X*Nz, 2 a = X + Y*Nx)
+int oracle_voxelize_rays(const OracleConfig* c, const u32 direction, void* fi, float* u, u8* flags, const u64 t, const u8 flag,
+                         const float* p0, const float* p1, const float* p2, const float* bbu, const u64* rays, const u64 nrays) {
+	return valid(c) && direction<3u && rays ? voxelize_impl(c, direction, fi, u, flags, t, flag, p0, p1, p2, bbu, rays, nrays) : -1;
 }
 int oracle_unvoxelize_mesh(const OracleConfig* c, u8* flags, const u8 flag, const float x0, const float y0, const float z0, const float x1, const float y1, const float z1) {
 	return valid(c) ? unvoxelize_impl(c, flags, flag, x0, y0, z0, x1, y1, z1) : -1;
