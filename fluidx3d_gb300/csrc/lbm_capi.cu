@@ -299,7 +299,7 @@ int lbm_domain_create(const lbm_config* c, lbm_domain** out) {
 	d->g.nx_inv = c->Nx==1u ? 0ull : (~0ull)/c->Nx+1ull; // ceil(2^64/Nx)
 	d->w = lbm_relaxation_rate(c->nu);
 	d->rates = make_rates(d->w);
-	// stream_collide implementation: FX3D_STREAM_COLLIDE_PATH=cells|rows|pairs|pipe|rowpairs forces one (diagnostics
+	// stream_collide implementation: FX3D_STREAM_COLLIDE_PATH=cells|rows|pairs|pipe forces one (diagnostics
 	// and tests); the default takes the two-cell packed kernel with per-thread prefetch for fast
 	// arithmetic on 16-bit storage where the lattice allows it (even Nx, fewer than 2^32 cells), else
 	// one thread per cell
@@ -308,7 +308,6 @@ int lbm_domain_create(const lbm_config* c, lbm_domain** out) {
 		else if(!std::strcmp(p, "rows")) d->path = PATH_ROWS;
 		else if(!std::strcmp(p, "pairs")) d->path = PATH_PAIRS;
 		else if(!std::strcmp(p, "pipe")) d->path = PATH_PIPE;
-		else if(!std::strcmp(p, "rowpairs")) d->path = PATH_ROWPAIRS;
 	}
 
 	cudaError_t e = cudaStreamCreateWithFlags(&d->own_stream, cudaStreamNonBlocking);

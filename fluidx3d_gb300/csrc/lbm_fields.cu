@@ -32,20 +32,6 @@ RowPlan row_plan(const int q, const int storage, const uint32_t Nx, const uint32
 	return p;
 }
 
-RowPlan rowpair_plan(const int q, const int storage, const uint32_t Nx, const uint32_t Ny, const uint32_t Nz) {
-	RowPlan p{0u, 0u, 0u};
-	const size_t elem = storage==ST_FP32 ? 4u : 2u;
-	if(Nx%16u!=0u || (uint64_t)Ny*Nz>0xFFFFFFFFull) return p;
-	const size_t stride = (Nx*elem+127u)&~(size_t)127u;
-	const size_t stage = (size_t)q*stride+((Nx+127u)&~(size_t)127u);
-	size_t k = (112u*1024u-128u)/stage;
-	if(k<3u) k = (224u*1024u-128u)/stage;
-	if(k<2u) return p;
-	if(k>6u) k = 6u;
-	p.stage_bytes = (uint32_t)stage; p.stages = (uint32_t)k; p.smem = (uint32_t)(k*stage+128u);
-	return p;
-}
-
 int persistent_grid(const void* kernel, const int threads, const size_t smem) {
 	struct Entry { const void* k; int threads; size_t smem; int dev; int grid; };
 	static Entry cache[64];

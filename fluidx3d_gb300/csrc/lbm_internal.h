@@ -48,14 +48,11 @@ constexpr int ROW_TPB_MAX = 512; // threads per CTA of the row-staged stream_col
 
 // stream_collide implementation: one thread per cell with direct global loads/stores ("cells"), or
 // one CTA per x-row with the row's slots staged in shared memory by bulk copies ("rows")
-enum : int { PATH_AUTO = 0, PATH_CELLS = 1, PATH_ROWS = 2, PATH_PAIRS = 3, PATH_PIPE = 4, PATH_ROWPAIRS = 5 };
+enum : int { PATH_AUTO = 0, PATH_CELLS = 1, PATH_ROWS = 2, PATH_PAIRS = 3, PATH_PIPE = 4 };
 // shared-memory plan of the row-staged kernel: bytes of one stage (one x-row's Q DDF rows + its flags)
 // and the number of stages; stages==0 if the lattice does not fit its constraints
 struct RowPlan { uint32_t stage_bytes, stages; size_t smem; };
 RowPlan row_plan(int q, int storage, uint32_t Nx, uint32_t Ny, uint32_t Nz);
-// stages of the warp-specialised two-cell row kernel: up to 6, two CTAs per SM if at least 3 fit in
-// 112 KB, else one CTA with up to 224 KB; 0 stages: not applicable (Nx%16, Nx even, Ny*Nz < 2^32)
-RowPlan rowpair_plan(int q, int storage, uint32_t Nx, uint32_t Ny, uint32_t Nz);
 inline size_t rows_smem_bytes(const int q, const int storage, const uint32_t Nx, const uint32_t Ny=1u, const uint32_t Nz=1u) {
 	return row_plan(q, storage, Nx, Ny, Nz).smem;
 }

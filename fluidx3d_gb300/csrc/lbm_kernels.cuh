@@ -501,174 +501,6 @@ k_stream_collide_rows(const StepArgs a, const uint32_t stages) {
 	if(copier) bulk_wait_all(); // stores complete before the CTA (and its shared memory) goes away
 }
 
-// Row-staged two-cell kernel, warp-specialised. The last warp of a CTA is the producer: for each
-// x-row of the CTA (rows r = blockIdx.x + j*gridDim.x) it bulk-loads the row's Q slot rows and its
-// flags row into stage j % stages (cp.async.bulk, completing on full[stage]) and, once the consumer
-// warps have arrived on done[stage], bulk-stores the slot rows to fi_dst and reloads the stage. The
-// consumer warps step two x-adjacent cells per thread from shared memory with the packed FP32x2
-// arithmetic and write the results back in place; warps meet only through the per-stage mbarriers,
-// never through a block-wide barrier. Global memory sees only whole 16-byte-aligned rows, so the
-// per-thread address arithmetic of the global-memory kernels disappears. Slot rows are as in
-// k_stream_collide_rows: slot row i (i odd) and 0 are the x-row's own slots, slot row i+1 the
-// neighbour row along c_i, rotated by c_ix. Fast arithmetic only; results are bit-identical to the
-// one-cell kernel. Every wait is bounded: a wait that runs out records KERR_MBARRIER_TIMEOUT, the
-// consumers stop, and the producer waits (bounded) for its copies in flight before returning.
-constexpr uint32_t RP_CONSUMER_WARPS = 8u;
-constexpr uint32_t RP_THREADS = 32u*(RP_CONSUMER_WARPS+1u);
-
-template<int ST> struct RowPairIO; // pairs and single values in a shared-memory slot row
-template<> struct RowPairIO<ST_FP32> {
-	static __device__ __forceinline__ float2 pair(const float* r, const uint32_t x) { return *reinterpret_cast<const float2*>(r+x); }
-	static __device__ __forceinline__ void put_pair(float* r, const uint32_t x, const float2 v) { *reinterpret_cast<float2*>(r+x) = v; }
-};
-template<> struct RowPairIO<ST_FP16S> {
-	static __device__ __forceinline__ float2 pair(const uint16_t* r, const uint32_t x) { return __half22float2(*reinterpret_cast<const __half2*>(r+x)); }
-	static __device__ __forceinline__ void put_pair(uint16_t* r, const uint32_t x, const float2 v) { *reinterpret_cast<__half2*>(r+x) = __float22half2_rn(v); }
-};
-template<> struct RowPairIO<ST_FP16C> {
-	static __device__ __forceinline__ float2 pair(const uint16_t* r, const uint32_t x) { return make_float2(RawCodec<ST_FP16C>::decode(r[x]), RawCodec<ST_FP16C>::decode(r[x+1u])); }
-	static __device__ __forceinline__ void put_pair(uint16_t* r, const uint32_t x, const float2 v) { r[x] = RawCodec<ST_FP16C>::encode(v.x); r[x+1u] = RawCodec<ST_FP16C>::encode(v.y); }
-};
-
-template<int Q, int ST, bool TRT, int EXT> __global__ void __launch_bounds__(RP_THREADS, (Q==19 ? 2 : 1))
-k_stream_collide_rowpairs(const StepArgs a, const uint32_t stages) {
-	typedef typename Codec<ST>::T T;
-	typedef RawCodec<ST> CD;
-	typedef RowPairIO<ST> IO;
-	constexpr bool EQ = (EXT&EXT_EQ)!=0, VF = (EXT&EXT_VF)!=0;
-	extern __shared__ __align__(128) unsigned char smem[];
-	__shared__ int abort_rows;
-	const Grid& g = grid_of(a.g);
-	const uint32_t Nx = g.Nx, Ny = g.Ny, Nz = g.Nz, rows = Ny*Nz;
-	const uint32_t warp = threadIdx.x>>5, lane = threadIdx.x&31u;
-	const RowStageLayout L(Q, (uint32_t)sizeof(T), Nx);
-	uint64_t* full = reinterpret_cast<uint64_t*>(smem);
-	uint64_t* done = full+stages;
-	unsigned char* stage0 = smem+128;
-	const bool odd = (a.t&1ull)!=0ull;
-	const uint64_t N = g.N;
-	const uint32_t nrows = rows>blockIdx.x ? (rows-1u-blockIdx.x)/gridDim.x+1u : 0u; // x-rows of this CTA
-	auto row_of = [&](const uint32_t j, uint32_t& y, uint32_t& z) { const uint32_t r = blockIdx.x+j*gridDim.x; z = r/Ny; y = r-z*Ny; };
-	if(threadIdx.x==0u) {
-		for(uint32_t s=0u; s<stages; s++) { mbar_init(full+s, 1u); mbar_init(done+s, RP_CONSUMER_WARPS); }
-		fence_mbar_init();
-		abort_rows = 0;
-	}
-	__syncthreads();
-	if(warp==RP_CONSUMER_WARPS) { // ---------------------------------------------------- producer warp
-		// lane k < Q moves slot row k, lane Q the flags row (Q <= 27 < 32)
-		uint32_t karr = 0u; int dy = 0, dz = 0;
-		if(lane<(uint32_t)Q && lane>0u) {
-			if(lane%2u==1u) karr = odd ? lane : lane+1u;
-			else { karr = odd ? lane : lane-1u; dy = c_vs_tab[1][lane-1u]; dz = c_vs_tab[2][lane-1u]; }
-		}
-		auto slot_row = [&](const uint32_t y, const uint32_t z) -> uint64_t {
-			const uint32_t yy = dy>0 ? (y+1u==Ny ? 0u : y+1u) : dy<0 ? (y==0u ? Ny-1u : y-1u) : y;
-			const uint32_t zz = dz>0 ? (z+1u==Nz ? 0u : z+1u) : dz<0 ? (z==0u ? Nz-1u : z-1u) : z;
-			return (uint64_t)karr*N+((uint64_t)zz*Ny+yy)*Nx;
-		};
-		auto load = [&](const uint32_t j) {
-			uint32_t y, z; row_of(j, y, z);
-			const uint32_t s = j%stages;
-			unsigned char* st = stage0+(size_t)s*L.stage_bytes;
-			if(lane==0u) mbar_arrive_expect_tx(full+s, (uint32_t)Q*L.rowbytes+Nx);
-			__syncwarp();
-			if(lane<(uint32_t)Q) bulk_load(st+(size_t)lane*L.stride, (const T*)a.fi+slot_row(y, z), L.rowbytes, full+s);
-			else if(lane==(uint32_t)Q) bulk_load(st+L.flags_off, a.flags+((uint64_t)z*Ny+y)*Nx, Nx, full+s);
-		};
-		auto store = [&](const uint32_t j) {
-			uint32_t y, z; row_of(j, y, z);
-			unsigned char* st = stage0+(size_t)(j%stages)*L.stage_bytes;
-			if(lane<(uint32_t)Q) { bulk_store((T*)a.fi_dst+slot_row(y, z), st+(size_t)lane*L.stride, L.rowbytes); bulk_commit(); }
-		};
-		auto drain = [&](const uint32_t loaded_from, const uint32_t loaded_to) { // after a wait ran out
-			if(lane==0u) for(uint32_t j=loaded_from; j<loaded_to; j++) mbar_wait_bounded(full+j%stages, (j/stages)&1u, nullptr);
-			if(lane<(uint32_t)Q) bulk_wait_all();
-		};
-		uint32_t j = 0u;
-		for(; j<nrows; j++) {
-			if(j>=stages) { // x-row j-stages held this stage: store it once the consumers are done with it
-				const uint32_t jo = j-stages;
-				bool ok = true;
-				if(lane==0u) ok = mbar_wait_bounded(done+jo%stages, (jo/stages)&1u, a.err);
-				ok = __shfl_sync(0xFFFFFFFFu, ok ? 1 : 0, 0)!=0;
-				if(!ok) { abort_rows = 1; drain(jo+1u, j); return; }
-				store(jo);
-				if(lane<(uint32_t)Q) bulk_wait_read_all(); // the stage has been read out before it is refilled
-				__syncwarp();
-			}
-			load(j);
-		}
-		for(uint32_t jo=nrows>stages ? nrows-stages : 0u; jo<nrows; jo++) { // the last rows
-			bool ok = true;
-			if(lane==0u) ok = mbar_wait_bounded(done+jo%stages, (jo/stages)&1u, a.err);
-			ok = __shfl_sync(0xFFFFFFFFu, ok ? 1 : 0, 0)!=0;
-			if(!ok) { abort_rows = 1; drain(jo+1u, nrows); return; }
-			store(jo);
-		}
-		if(lane<(uint32_t)Q) bulk_wait_all(); // stores complete before the CTA (and its shared memory) goes away
-		return;
-	}
-	// ---------------------------------------------------------------------------------- consumer warps
-	for(uint32_t j=0u; j<nrows; j++) {
-		const uint32_t s = j%stages;
-		if(!mbar_wait_bounded(full+s, (j/stages)&1u, a.err)) { abort_rows = 1; return; }
-		if(*(volatile int*)&abort_rows) return;
-		unsigned char* st = stage0+(size_t)s*L.stage_bytes;
-		auto srow = [&](const int k) { return reinterpret_cast<T*>(st+(size_t)k*L.stride); };
-		const uint8_t* fl = st+L.flags_off;
-		uint32_t y, z; row_of(j, y, z);
-		const uint64_t row0 = ((uint64_t)z*Ny+y)*Nx;
-		for(uint32_t x0=2u*threadIdx.x; x0<Nx; x0+=2u*32u*RP_CONSUMER_WARPS) {
-			const uint32_t fa = fl[x0], fb = fl[x0+1u];
-			const bool skip_a = (fa&TYPE_BO)==TYPE_S||(fa&TYPE_SU)==TYPE_G, skip_b = (fb&TYPE_BO)==TYPE_S||(fb&TYPE_SU)==TYPE_G;
-			if(skip_a&&skip_b) continue;
-			const uint32_t xm = x0==0u ? Nx-1u : x0-1u, xp2 = x0+2u==Nx ? 0u : x0+2u; // wrapped neighbours of the pair
-			float2 f[Q];
-			f[0] = IO::pair(srow(0), x0);
-			Unroll<1, Q, 2>::run([&](auto ic) {
-				constexpr int i = decltype(ic)::value, cx = vs_c(0, i);
-				f[i] = IO::pair(srow(i), x0);
-				if constexpr(cx==0) f[i+1] = IO::pair(srow(i+1), x0);
-				else if constexpr(cx>0) f[i+1] = make_float2(CD::decode(srow(i+1)[x0+1u]), CD::decode(srow(i+1)[xp2]));
-				else f[i+1] = make_float2(CD::decode(srow(i+1)[xm]), CD::decode(srow(i+1)[x0]));
-			});
-			if(skip_a||skip_b) { // one cell of the pair steps alone
-				const uint32_t c = skip_a ? 1u : 0u, x = x0+c;
-				const uint32_t xpc = x+1u==Nx ? 0u : x+1u, xmc = x==0u ? Nx-1u : x-1u;
-				float f1[Q];
-				#pragma unroll
-				for(int k=0; k<Q; k++) f1[k] = c ? f[k].y : f[k].x;
-				cell_step<Q, ST, TRT, EXT, true>(f1, a, row0+x, EQ && ((skip_a ? fb : fa)&TYPE_BO)==TYPE_E);
-				srow(0)[x] = CD::encode(f1[0]);
-				Unroll<1, Q, 2>::run([&](auto ic) {
-					constexpr int i = decltype(ic)::value, cx = vs_c(0, i);
-					srow(i+1)[cx>0 ? xpc : cx<0 ? xmc : x] = CD::encode(f1[i]);
-					srow(i)[x] = CD::encode(f1[i+1]);
-				});
-				continue;
-			}
-			const Bool2 is_e{EQ && (fa&TYPE_BO)==TYPE_E, EQ && (fb&TYPE_BO)==TYPE_E};
-			const bool any_e = is_e.x||is_e.y;
-			float2 R, Rm1, inv, ux, uy, uz, fx, fy, fz;
-			cell_rho_u_v<Q, EXT, ST, float2>(a, row0+x0, f, is_e, any_e, R, Rm1, inv, ux, uy, uz, fx, fy, fz);
-			if(any_e) collide_v<Q, TRT, VF, ST, 2>(f, R, Rm1, ux, uy, uz, fx, fy, fz, is_e, a);
-			else collide_v<Q, TRT, VF, ST, 0>(f, R, Rm1, ux, uy, uz, fx, fy, fz, is_e, a);
-			IO::put_pair(srow(0), x0, f[0]);
-			Unroll<1, Q, 2>::run([&](auto ic) {
-				constexpr int i = decltype(ic)::value, cx = vs_c(0, i);
-				if constexpr(cx==0) IO::put_pair(srow(i+1), x0, f[i]);
-				else if constexpr(cx>0) { srow(i+1)[x0+1u] = CD::encode(f[i].x); srow(i+1)[xp2] = CD::encode(f[i].y); }
-				else { srow(i+1)[xm] = CD::encode(f[i].x); srow(i+1)[x0] = CD::encode(f[i].y); }
-				IO::put_pair(srow(i), x0, f[i+1]);
-			});
-		}
-		fence_proxy_async_smem(); // this thread's writes before the producer's bulk stores read the stage
-		__syncwarp();
-		if(lane==0u) mbar_arrive(done+s);
-	}
-}
-
 template<int Q, int ST, int EXT, bool FAST> __global__ void __launch_bounds__(BLOCK) k_update_fields(const StepArgs a) {
 	typedef typename Codec<ST>::T T;
 	constexpr bool EQ = (EXT&EXT_EQ)!=0;
@@ -728,22 +560,6 @@ template<int ST, int Q, bool TRT, int EXT, bool FAST> inline cudaError_t sc_laun
 		int grid = persistent_grid((const void*)kernel, tpb, plan.smem);
 		if((uint64_t)grid>rows_total) grid = (int)rows_total;
 		kernel<<<grid, tpb, plan.smem, s>>>(a, plan.stages);
-	} else if(kind==PATH_ROWPAIRS) {
-		if constexpr(FAST) {
-			const RowPlan plan = rowpair_plan(Q, ST, a.g.Nx, a.g.Ny, a.g.Nz);
-			if(plan.stages==0u) return cudaErrorInvalidConfiguration;
-			auto kernel = k_stream_collide_rowpairs<Q, ST, TRT, EXT>;
-			if(plan.smem>48u*1024u) {
-				const cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)plan.smem);
-				if(e!=cudaSuccess) return e;
-			}
-			const uint64_t rows_total = (uint64_t)a.g.Ny*a.g.Nz;
-			int grid = persistent_grid((const void*)kernel, (int)RP_THREADS, plan.smem);
-			if((uint64_t)grid>rows_total) grid = (int)rows_total;
-			kernel<<<grid, RP_THREADS, plan.smem, s>>>(a, plan.stages);
-		} else {
-			return cudaErrorInvalidConfiguration; // the packed kernels have fast arithmetic only
-		}
 	} else if(kind==PATH_PAIRS||kind==PATH_PIPE) {
 		if constexpr(FAST) {
 			if(a.fi_dst!=a.fi||!pairs_supported(a.g)) return cudaErrorInvalidValue; // in place, even Nx, N < 2^32
@@ -790,9 +606,7 @@ template<int ST> cudaError_t launch_stream_collide_t(const Variant& v, const Ste
 	const bool pairs_ok = v.fast && pairs_supported(a.g) && a.fi_dst==a.fi;
 	int kind = path;
 	if(path==PATH_AUTO) kind = pairs_ok && ST!=ST_FP32 ? PATH_PIPE : PATH_CELLS;
-	const bool rowpairs_ok = v.fast && rowpair_plan(v.q, ST, a.g.Nx, a.g.Ny, a.g.Nz).stages!=0u;
-	if((kind==PATH_ROWS && !rows_ok) || ((kind==PATH_PAIRS||kind==PATH_PIPE) && !pairs_ok) || (kind==PATH_ROWPAIRS && !rowpairs_ok))
-		return cudaErrorInvalidConfiguration;
+	if((kind==PATH_ROWS && !rows_ok) || ((kind==PATH_PAIRS||kind==PATH_PIPE) && !pairs_ok)) return cudaErrorInvalidConfiguration;
 	if(v.q==19) return v.trt ? sc_ext<ST, 19, true>(v.ext, a, kind, v.fast, s) : sc_ext<ST, 19, false>(v.ext, a, kind, v.fast, s);
 	if(v.q==27) return v.trt ? sc_ext<ST, 27, true>(v.ext, a, kind, v.fast, s) : sc_ext<ST, 27, false>(v.ext, a, kind, v.fast, s);
 	return cudaErrorInvalidValue;
