@@ -40,7 +40,7 @@ typedef uint32_t u32;
 typedef uint64_t u64;
 
 enum { ST_FP32 = 0, ST_FP16S = 1, ST_FP16C = 2 };
-enum { EXT_VOLUME_FORCE = 1, EXT_FORCE_FIELD = 2, EXT_EQUILIBRIUM_BOUNDARIES = 4 };
+enum { EXT_VOLUME_FORCE = 1, EXT_FORCE_FIELD = 2, EXT_EQUILIBRIUM_BOUNDARIES = 4, EXT_SUBGRID = 8 };
 enum { T_S = 0x01, T_E = 0x02, T_BO = 0x03, T_MS = 0x03, T_G = 0x20, T_SU = 0x38, T_XY = 0xC0 };
 
 extern "C" struct OracleConfig {
@@ -269,7 +269,19 @@ template<typename real> static void collide_cell(real* fhn, const real rhon, con
 	real Fin[27], feq[27];
 	if(vf) forcing_terms<real>(uxn, uyn, uzn, fxn, fyn, fzn, Fin, q); else for(u32 i=0u; i<q; i++) Fin[i] = (real)0;
 	calculate_f_eq<real>(rhon, uxn, uyn, uzn, feq, q);
-	const real w = (real)c->w;
+	real w = (real)c->w;
+	if(c->ext&EXT_SUBGRID) { // Smagorinsky-Lilly relaxation rate of this cell (src/kernel.cpp:1579-1593)
+		const real tau0 = (real)1/w;
+		real Hxx = 0, Hyy = 0, Hzz = 0, Hxy = 0, Hxz = 0, Hyz = 0; // non-equilibrium stress tensor
+		for(u32 i=1u; i<q; i++) {
+			const real fneqi = fhn[i]-feq[i];
+			const real cxi = (real)cq(q, 0, i), cyi = (real)cq(q, 1, i), czi = (real)cq(q, 2, i);
+			Hxx += cxi*cxi*fneqi; Hxy += cxi*cyi*fneqi; Hyy += cyi*cyi*fneqi;
+			Hxz += cxi*czi*fneqi; Hyz += cyi*czi*fneqi; Hzz += czi*czi*fneqi;
+		}
+		const real Qs = Hxx*Hxx+Hyy*Hyy+Hzz*Hzz+(real)2*(Hxy*Hxy+Hxz*Hxz+Hyz*Hyz);
+		w = (real)2/(tau0+std::sqrt(tau0*tau0+(real)0.76421222f*std::sqrt(Qs)/rhon));
+	}
 	if(!c->trt) { // SRT (src/kernel.cpp:1595-1604)
 		if(vf) { const real c_tau = fmaT(w, (real)(-0.5), (real)1); for(u32 i=0u; i<q; i++) Fin[i] *= c_tau; }
 		for(u32 i=0u; i<q; i++) fhn[i] = is_e ? feq[i] : fmaT((real)1-w, fhn[i], fmaT(w, feq[i], Fin[i]));

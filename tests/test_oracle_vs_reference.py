@@ -20,7 +20,8 @@ def _harness(variant):
 
 
 VARIANTS = [(19, "srt", "fp32", ("eq", "ff", "vf")), (19, "trt", "fp16s", ("eq", "ff", "vf")), (19, "srt", "fp16c", ("eq",)),
-            (27, "trt", "fp32", ("eq", "ff", "vf")), (27, "srt", "fp16s", ())]
+            (27, "trt", "fp32", ("eq", "ff", "vf")), (27, "srt", "fp16s", ()),
+            (19, "srt", "fp32", ("sg",)), (19, "trt", "fp16s", ("eq", "sg")), (27, "trt", "fp32", ("eq", "ff", "sg", "vf"))]
 
 
 @pytest.mark.parametrize("variant", VARIANTS, ids=["_".join([str(v[0]), v[1], v[2], *v[3]]) for v in VARIANTS])
