@@ -263,7 +263,7 @@ int lbm_domain_create(const lbm_config* c, lbm_domain** out) {
 	if(c->velocity_set!=19u&&c->velocity_set!=27u) return fail(LBM_ERR_INVALID_ARGUMENT, "velocity_set must be 19 or 27, got %u", c->velocity_set);
 	if(c->collision>LBM_TRT) return fail(LBM_ERR_INVALID_ARGUMENT, "collision must be LBM_SRT or LBM_TRT");
 	if(c->storage>LBM_FP16C) return fail(LBM_ERR_INVALID_ARGUMENT, "storage must be LBM_FP32, LBM_FP16S or LBM_FP16C");
-	if(c->extensions&~7u) return fail(LBM_ERR_INVALID_ARGUMENT, "unknown extension bits 0x%x", c->extensions&~7u);
+	if(c->extensions&~15u) return fail(LBM_ERR_INVALID_ARGUMENT, "unknown extension bits 0x%x", c->extensions&~15u);
 	if(c->arithmetic>LBM_ARITH_FAST) return fail(LBM_ERR_INVALID_ARGUMENT, "arithmetic must be LBM_ARITH_AUTO, LBM_ARITH_EXACT or LBM_ARITH_FAST");
 	if(!(c->nu>0.0f)) return fail(LBM_ERR_INVALID_ARGUMENT, c->nu==0.0f ? "Viscosity cannot be 0." : "Viscosity cannot be negative.");
 	if(!(c->extensions&LBM_EXT_VOLUME_FORCE)&&(c->fx!=0.0f||c->fy!=0.0f||c->fz!=0.0f))
@@ -293,6 +293,7 @@ int lbm_domain_create(const lbm_config* c, lbm_domain** out) {
 	if(c->extensions&LBM_EXT_VOLUME_FORCE) ext |= EXT_VF;
 	if((c->extensions&LBM_EXT_FORCE_FIELD)&&(c->extensions&LBM_EXT_VOLUME_FORCE)) ext |= EXT_FF; // F acts on the fluid only with VOLUME_FORCE
 	if(c->extensions&LBM_EXT_EQUILIBRIUM_BOUNDARIES) ext |= EXT_EQ;
+	if(c->extensions&LBM_EXT_SUBGRID) ext |= EXT_SG;
 	d->v.ext = ext;
 	d->v.fast = c->arithmetic==LBM_ARITH_FAST || (c->arithmetic==LBM_ARITH_AUTO && c->storage!=LBM_FP32);
 	d->g.Nx = c->Nx; d->g.Ny = c->Ny; d->g.Nz = c->Nz; d->g.NxNy = c->Nx*c->Ny; d->g.N = N;
@@ -598,6 +599,7 @@ extern "C" int lbm_run_adjoint(lbm_domain* d, const lbm_adjoint_config* cfg, dou
 	FX3D_DOMAIN(d);
 	if(!cfg) return fail(LBM_ERR_INVALID_ARGUMENT, "lbm_run_adjoint: NULL config");
 	if(!d->initialized) return fail(LBM_ERR_NOT_INITIALIZED, "lbm_run_adjoint: call lbm_initialize first");
+	if(d->v.ext&EXT_SG) return fail(LBM_ERR_UNSUPPORTED, "lbm_run_adjoint does not support LBM_EXT_SUBGRID (the adjoint has no Smagorinsky-Lilly term)");
 	if(!adjoint_supported(d->v) || !d->F) return fail(LBM_ERR_UNSUPPORTED, "lbm_run_adjoint needs LBM_EXT_VOLUME_FORCE and LBM_EXT_FORCE_FIELD (F is the design variable)");
 	if(d->g.N>0xFFFFFFFFull) return fail(LBM_ERR_UNSUPPORTED, "lbm_run_adjoint needs fewer than 2^32 cells (its kernels use 32-bit cell indices)");
 	if(cfg->steps==0ull||cfg->checkpoint_interval==0ull) return fail(LBM_ERR_INVALID_ARGUMENT, "lbm_run_adjoint: steps and checkpoint_interval must be >= 1");

@@ -192,10 +192,61 @@ template<int Q, int EXT, int ST, class V, class M> __device__ __forceinline__ vo
 	}
 }
 
+// collision rates as values of V: uniform (the host's rates) or per cell (SUBGRID)
+template<class V> struct VRates {
+	V w, hp, hm, nhm, half_c_tau, c_taup, c_taum;
+	V rest_rate, rest_force; // the rest direction's relaxation and Guo factors (SRT: w, c_tau; TRT: 2 hp, 2 c_taup)
+};
+struct LaneRates { float w, hp, hm, nhm, half_c_tau, c_taup, c_taum, rest_rate, rest_force; };
+template<bool TRT> __device__ __forceinline__ LaneRates lane_rates(const float w, const float hp, const float hm, const float c_tau, const float c_taup,
+                                                                 const float c_taum) {
+	return LaneRates{w, hp, hm, -hm, 0.5f*c_tau, c_taup, c_taum, !TRT ? w : 2.0f*hp, !TRT ? c_tau : 2.0f*c_taup};
+}
+template<class V> __device__ __forceinline__ VRates<V> v_rates(const LaneRates& a);
+template<> __device__ __forceinline__ VRates<float> v_rates<float>(const LaneRates& a) {
+	return VRates<float>{a.w, a.hp, a.hm, a.nhm, a.half_c_tau, a.c_taup, a.c_taum, a.rest_rate, a.rest_force};
+}
+__device__ __forceinline__ VRates<float2> v_rates2(const LaneRates& a, const LaneRates& b) {
+	return VRates<float2>{make_float2(a.w, b.w), make_float2(a.hp, b.hp), make_float2(a.hm, b.hm), make_float2(a.nhm, b.nhm),
+	                      make_float2(a.half_c_tau, b.half_c_tau), make_float2(a.c_taup, b.c_taup), make_float2(a.c_taum, b.c_taum),
+	                      make_float2(a.rest_rate, b.rest_rate), make_float2(a.rest_force, b.rest_force)};
+}
+template<> __device__ __forceinline__ VRates<float2> v_rates<float2>(const LaneRates& a) { return v_rates2(a, a); }
+// SUBGRID rates of one cell from its stress tensor H (storage units) and 1/R, with the hardware
+// approximations of sqrt and 1/x: tau = (tau0 + sqrt(tau0^2 + 0.76421222 sqrt(H:H)/rho))/2,
+// w = 1/tau (the reference's 2/(tau0 + ...)), TRT: wm = 1/(0.1875/(tau - 1/2) + 1/2)
+__device__ __forceinline__ float approx_rcp(const float x) { float y; asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x)); return y; }
+__device__ __forceinline__ float approx_sqrt(const float x) { float y; asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x)); return y; }
+template<bool TRT> __device__ __forceinline__ LaneRates subgrid_lane_rates(const float tau0, const float* H, const float inv) {
+	const float diag = __fmaf_rn(H[0], H[0], __fmaf_rn(H[1], H[1], __fmul_rn(H[2], H[2])));
+	const float Qs = __fmaf_rn(2.0f, __fmaf_rn(H[3], H[3], __fmaf_rn(H[4], H[4], __fmul_rn(H[5], H[5]))), diag);
+	const float S = approx_sqrt(__fmaf_rn(__fmul_rn(0.76421222f, approx_sqrt(Qs)), inv, __fmul_rn(tau0, tau0)));
+	const float tau = __fmul_rn(0.5f, __fadd_rn(tau0, S));
+	const float w = approx_rcp(tau);
+	const float wm = TRT ? approx_rcp(__fmaf_rn(0.1875f, approx_rcp(__fsub_rn(tau, 0.5f)), 0.5f)) : w;
+	return lane_rates<TRT>(w, __fmul_rn(0.5f, w), __fmul_rn(0.5f, wm), __fmaf_rn(w, -0.5f, 1.0f), __fmaf_rn(w, -0.25f, 0.5f), __fmaf_rn(wm, -0.25f, 0.5f));
+}
+// stress contribution of the opposite pair (I, I+1): both directions share c c^T, so their pair sum
+// of non-equilibrium parts s enters once
+template<int I, class V> __device__ __forceinline__ void stress_add_v(V* H, const V s) {
+	constexpr int cx = vs_c(0, I), cy = vs_c(1, I), cz = vs_c(2, I);
+	if constexpr(cx!=0) H[0] = v_add(H[0], s);
+	if constexpr(cy!=0) H[1] = v_add(H[1], s);
+	if constexpr(cz!=0) H[2] = v_add(H[2], s);
+	if constexpr(cx!=0 && cy!=0) H[3] = cx*cy>0 ? v_add(H[3], s) : v_sub(H[3], s);
+	if constexpr(cx!=0 && cz!=0) H[4] = cx*cz>0 ? v_add(H[4], s) : v_sub(H[4], s);
+	if constexpr(cy!=0 && cz!=0) H[5] = cy*cz>0 ? v_add(H[5], s) : v_sub(H[5], s);
+}
+
 // collision of all directions in place, DDFs in storage units (K scaling). EMODE 0: no TYPE_E cell;
-// 1: the (single) cell is TYPE_E (f = feq); 2: mixed lanes, TYPE_E lanes picked by is_e.
-template<int Q, bool TRT, bool VF, int ST, int EMODE, class V, class M> __device__ __forceinline__ void collide_v(V* f, const V R, const V Rm1, const V ux, const V uy,
-                                                                                                             const V uz, const V fx, const V fy, const V fz,
+// 1: the (single) cell is TYPE_E (f = feq); 2: mixed lanes, TYPE_E lanes picked by is_e. SG: the
+// relaxation rate of each cell from the Smagorinsky-Lilly model (src/kernel.cpp:1579-1593); the
+// stress tensor comes from pair sums f_i + f_j - (feq_i + feq_j), feq_i + feq_j = 2 base, and the
+// rate itself from the same scalar operations in either form of V (sqrt(H:H)/rho is the same in
+// storage units, H and R both carry the factor K).
+template<int Q, bool TRT, bool VF, int ST, int EMODE, class V, class M, bool SG = false> __device__ __forceinline__ void collide_v(V* f, const V R, const V Rm1,
+                                                                                                             const V ux, const V uy, const V uz,
+                                                                                                             const V fx, const V fy, const V fz,
                                                                                                              const M is_e, const StepArgs& a) {
 	constexpr float K = RawCodec<ST>::K;
 	const V c3 = v_mul(v_set<V>(-3.0f), v_fma(ux, ux, v_fma(uy, uy, v_mul(uz, uz))));
@@ -205,16 +256,6 @@ template<int Q, bool TRT, bool VF, int ST, int EMODE, class V, class M> __device
 		fxK = v_mul(v_set<V>(K), fx); fyK = v_mul(v_set<V>(K), fy); fzK = v_mul(v_set<V>(K), fz);
 		uF = v_mul(v_set<V>(-THIRD), v_fma(ux, fxK, v_fma(uy, fyK, v_mul(uz, fzK))));
 	}
-	{ // center: feq_0 = w_0 X; its difference to f_0 as one fused operation
-		const V X = v_fma(R, v_mul(v_set<V>(0.5f), c3), Rm1), w0 = v_set<V>(vs_w<Q>(0));
-		if constexpr(EMODE==1) f[0] = v_mul(w0, X);
-		else {
-			const V d0 = v_fma(w0, X, v_neg(f[0]));
-			V g0 = v_fma(v_set<V>(!TRT ? a.w : 2.0f*a.hp), d0, f[0]);
-			if constexpr(VF) g0 = v_fma(v_set<V>(!TRT ? a.c_tau : 2.0f*a.c_taup), v_mul(v_set<V>(9.0f*vs_w<Q>(0)), uF), g0);
-			if constexpr(EMODE==2) f[0] = v_pick(g0, v_mul(w0, X), is_e); else f[0] = g0;
-		}
-	}
 	// w R, w R / 2 and w (R-K) once per weight class (straight, edge, corner directions)
 	constexpr int NC = Q==27 ? 3 : 2;
 	V rwc[NC], nrwc[NC], hrc[NC], wmc[NC];
@@ -223,34 +264,71 @@ template<int Q, bool TRT, bool VF, int ST, int EMODE, class V, class M> __device
 		const float wc = vs_w<Q>(c==0 ? 1 : c==1 ? 7 : 19);
 		rwc[c] = v_mul(v_set<V>(wc), R); nrwc[c] = v_mul(v_set<V>(-wc), R); hrc[c] = v_mul(v_set<V>(0.5f*wc), R); wmc[c] = v_mul(v_set<V>(wc), Rm1);
 	}
+	auto base_of = [&](auto ic, V& uk) { // the shared equilibrium term of pair (i, i+1)
+		constexpr int i = decltype(ic)::value;
+		constexpr int c = (vs_c(0, i)!=0)+(vs_c(1, i)!=0)+(vs_c(2, i)!=0)-1;
+		uk = csum_v<i>(ux3, uy3, uz3);
+		return v_fma(hrc[c], v_fma(uk, uk, c3), wmc[c]);
+	};
+	VRates<V> r;
+	if constexpr(SG) {
+		V H[6];
+		#pragma unroll
+		for(int k=0; k<6; k++) H[k] = v_set<V>(0.0f);
+		Unroll<1, Q, 2>::run([&](auto ic) {
+			constexpr int i = decltype(ic)::value;
+			V uk;
+			const V base = base_of(ic, uk);
+			stress_add_v<i>(H, v_sub(v_add(f[i], f[i+1]), v_add(base, base)));
+		});
+		const float tau0 = __fdiv_rn(1.0f, a.w); // uniform
+		const V inv = v_rcp(R);
+		if constexpr(std::is_same<V, float>::value) {
+			r = v_rates<V>(subgrid_lane_rates<TRT>(tau0, H, inv));
+		} else {
+			const float Ha[6] = {H[0].x, H[1].x, H[2].x, H[3].x, H[4].x, H[5].x}, Hb[6] = {H[0].y, H[1].y, H[2].y, H[3].y, H[4].y, H[5].y};
+			r = v_rates2(subgrid_lane_rates<TRT>(tau0, Ha, inv.x), subgrid_lane_rates<TRT>(tau0, Hb, inv.y));
+		}
+	} else {
+		r = v_rates<V>(lane_rates<TRT>(a.w, a.hp, a.hm, a.c_tau, a.c_taup, a.c_taum));
+	}
+	{ // center: feq_0 = w_0 X; its difference to f_0 as one fused operation
+		const V X = v_fma(R, v_mul(v_set<V>(0.5f), c3), Rm1), w0 = v_set<V>(vs_w<Q>(0));
+		if constexpr(EMODE==1) f[0] = v_mul(w0, X);
+		else {
+			const V d0 = v_fma(w0, X, v_neg(f[0]));
+			V g0 = v_fma(r.rest_rate, d0, f[0]);
+			if constexpr(VF) g0 = v_fma(r.rest_force, v_mul(v_set<V>(9.0f*vs_w<Q>(0)), uF), g0);
+			if constexpr(EMODE==2) f[0] = v_pick(g0, v_mul(w0, X), is_e); else f[0] = g0;
+		}
+	}
 	Unroll<1, Q, 2>::run([&](auto ic) {
 		constexpr int i = decltype(ic)::value;
 		constexpr int c = (vs_c(0, i)!=0)+(vs_c(1, i)!=0)+(vs_c(2, i)!=0)-1;
 		const float wi = vs_w<Q>(i);
-		const V rw = rwc[c];
-		const V uk = csum_v<i>(ux3, uy3, uz3);
-		const V base = v_fma(hrc[c], v_fma(uk, uk, c3), wmc[c]);
-		const V ea = v_fma(rw, uk, base), eb = v_fma(nrwc[c], uk, base);
+		V uk;
+		const V base = base_of(ic, uk);
+		const V ea = v_fma(rwc[c], uk, base), eb = v_fma(nrwc[c], uk, base);
 		if constexpr(EMODE==1) { f[i] = ea; f[i+1] = eb; }
 		else {
 			const V da = v_sub(ea, f[i]), db = v_sub(eb, f[i+1]);
 			V na, nb;
-			if constexpr(!TRT) { na = v_fma(v_set<V>(a.w), da, f[i]); nb = v_fma(v_set<V>(a.w), db, f[i+1]); }
+			if constexpr(!TRT) { na = v_fma(r.w, da, f[i]); nb = v_fma(r.w, db, f[i+1]); }
 			else {
-				const V t = v_mul(v_set<V>(a.hp), v_add(da, db)), dd = v_sub(da, db);
-				na = v_add(f[i], v_fma(v_set<V>(a.hm), dd, t)); nb = v_add(f[i+1], v_fma(v_set<V>(-a.hm), dd, t));
+				const V t = v_mul(r.hp, v_add(da, db)), dd = v_sub(da, db);
+				na = v_add(f[i], v_fma(r.hm, dd, t)); nb = v_add(f[i+1], v_fma(r.nhm, dd, t));
 			}
 			if constexpr(VF) {
 				const V cf = csum_v<i>(fxK, fyK, fzK);
 				const V Y = v_fma(cf, v_mul(uk, v_set<V>(THIRD)), uF);
 				const V gd = v_mul(v_set<V>(6.0f*wi), cf);                     // G_i - G_j
 				if constexpr(!TRT) { // G_i = gs + gd and G_j = gs - gd, each one fused operation
-					na = v_fma(v_set<V>(0.5f*a.c_tau), v_fma(v_set<V>(18.0f*wi), Y, gd), na);
-					nb = v_fma(v_set<V>(0.5f*a.c_tau), v_fma(v_set<V>(18.0f*wi), Y, v_neg(gd)), nb);
+					na = v_fma(r.half_c_tau, v_fma(v_set<V>(18.0f*wi), Y, gd), na);
+					nb = v_fma(r.half_c_tau, v_fma(v_set<V>(18.0f*wi), Y, v_neg(gd)), nb);
 				} else {
 					const V gs = v_mul(v_set<V>(18.0f*wi), Y);                 // G_i + G_j  (c.u = uk/3)
-					const V m = v_mul(v_set<V>(a.c_taum), gd);
-					na = v_add(na, v_fma(v_set<V>(a.c_taup), gs, m)); nb = v_add(nb, v_fma(v_set<V>(a.c_taup), gs, v_neg(m)));
+					const V m = v_mul(r.c_taum, gd);
+					na = v_add(na, v_fma(r.c_taup, gs, m)); nb = v_add(nb, v_fma(r.c_taup, gs, v_neg(m)));
 				}
 			}
 			if constexpr(EMODE==2) { f[i] = v_pick(na, ea, is_e); f[i+1] = v_pick(nb, eb, is_e); }
@@ -265,11 +343,11 @@ template<int Q, int EXT, int ST> __device__ __forceinline__ void cell_rho_u_fast
                                                                                 float& fx, float& fy, float& fz) {
 	cell_rho_u_v<Q, EXT, ST, float>(a, n, f, is_e, is_e, R, Rm1, inv, ux, uy, uz, fx, fy, fz);
 }
-template<int Q, bool TRT, bool VF, int ST> __device__ __forceinline__ void collide_fast(float* f, const float R, const float Rm1, const float ux, const float uy,
-                                                                                      const float uz, const float fx, const float fy, const float fz,
-                                                                                      const bool is_e, const StepArgs& a) {
-	if(is_e) collide_v<Q, TRT, VF, ST, 1>(f, R, Rm1, ux, uy, uz, fx, fy, fz, is_e, a);
-	else collide_v<Q, TRT, VF, ST, 0>(f, R, Rm1, ux, uy, uz, fx, fy, fz, is_e, a);
+template<int Q, bool TRT, bool VF, int ST, bool SG = false> __device__ __forceinline__ void collide_fast(float* f, const float R, const float Rm1, const float ux,
+                                                                                                      const float uy, const float uz, const float fx, const float fy,
+                                                                                                      const float fz, const bool is_e, const StepArgs& a) {
+	if(is_e) collide_v<Q, TRT, VF, ST, 1, float, bool, SG>(f, R, Rm1, ux, uy, uz, fx, fy, fz, is_e, a);
+	else collide_v<Q, TRT, VF, ST, 0, float, bool, SG>(f, R, Rm1, ux, uy, uz, fx, fy, fz, is_e, a);
 }
 
 } // namespace fx3d

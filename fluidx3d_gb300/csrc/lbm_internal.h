@@ -6,7 +6,7 @@
 namespace fx3d {
 
 enum : int { ST_FP32 = 0, ST_FP16S = 1, ST_FP16C = 2 }; // DDF storage formats
-enum : int { EXT_VF = 1, EXT_FF = 2, EXT_EQ = 4 };          // VOLUME_FORCE, FORCE_FIELD, EQUILIBRIUM_BOUNDARIES
+enum : int { EXT_VF = 1, EXT_FF = 2, EXT_EQ = 4, EXT_SG = 8 }; // VOLUME_FORCE, FORCE_FIELD, EQUILIBRIUM_BOUNDARIES, SUBGRID
 
 struct GridDesc { // mirrors fx3d::Grid of lbm_scheme.cuh (kept layout-identical)
 	uint32_t Nx, Ny, Nz, NxNy;

@@ -72,16 +72,24 @@ template<int Q, int EXT> __device__ __forceinline__ void cell_rho_u(const StepAr
 }
 
 // one cell step on registers: f in, f out (exact: real units; fast: storage units)
+// (SUBGRID: the cell's relaxation rate from the Smagorinsky-Lilly model, src/kernel.cpp:1579-1593)
 template<int Q, int ST, bool TRT, int EXT, bool FAST> __device__ __forceinline__ void cell_step(float* f, const StepArgs& a, const uint64_t n, const bool is_e) {
-	constexpr bool VF = (EXT&EXT_VF)!=0;
+	constexpr bool VF = (EXT&EXT_VF)!=0, SG = (EXT&EXT_SG)!=0;
 	float rho, ux, uy, uz, fx, fy, fz;
 	if constexpr(FAST) {
 		float rm1, inv;
 		cell_rho_u_fast<Q, EXT, ST>(a, n, f, is_e, rho, rm1, inv, ux, uy, uz, fx, fy, fz);
-		collide_fast<Q, TRT, VF, ST>(f, rho, rm1, ux, uy, uz, fx, fy, fz, is_e, a);
+		collide_fast<Q, TRT, VF, ST, SG>(f, rho, rm1, ux, uy, uz, fx, fy, fz, is_e, a);
 	} else {
 		cell_rho_u<Q, EXT>(a, n, f, is_e, rho, ux, uy, uz, fx, fy, fz);
-		collide<Q, TRT, VF>(f, rho, ux, uy, uz, fx, fy, fz, is_e, a);
+		if constexpr(SG) {
+			StepArgs b = a; // the same step with this cell's rates
+			b.w = subgrid_w_exact<Q>(f, eq_state(rho, ux, uy, uz), a.w);
+			cell_rates(b.w, b.omw, b.c_tau, b.hp, b.hm, b.c_taup, b.c_taum);
+			collide<Q, TRT, VF>(f, rho, ux, uy, uz, fx, fy, fz, is_e, b);
+		} else {
+			collide<Q, TRT, VF>(f, rho, ux, uy, uz, fx, fy, fz, is_e, a);
+		}
 	}
 }
 template<int ST, bool FAST> using StepCodec = typename std::conditional<FAST, RawCodec<ST>, Codec<ST>>::type;
@@ -208,8 +216,8 @@ template<int Q, int ST, bool TRT, int EXT> __global__ void __launch_bounds__(BLO
 	const bool any_e = is_e.x||is_e.y;
 	float2 R, Rm1, inv, ux, uy, uz, fx, fy, fz;
 	cell_rho_u_v<Q, EXT, ST, float2>(a, n, f, is_e, any_e, R, Rm1, inv, ux, uy, uz, fx, fy, fz);
-	if(any_e) collide_v<Q, TRT, VF, ST, 2>(f, R, Rm1, ux, uy, uz, fx, fy, fz, is_e, a);
-	else collide_v<Q, TRT, VF, ST, 0>(f, R, Rm1, ux, uy, uz, fx, fy, fz, is_e, a);
+	if(any_e) collide_v<Q, TRT, VF, ST, 2, float2, Bool2, (EXT&EXT_SG)!=0>(f, R, Rm1, ux, uy, uz, fx, fy, fz, is_e, a);
+	else collide_v<Q, TRT, VF, ST, 0, float2, Bool2, (EXT&EXT_SG)!=0>(f, R, Rm1, ux, uy, uz, fx, fy, fz, is_e, a);
 	store_pair<Q, ST>((T*)a.fi, g.N, sa, sb, odd, f);
 }
 
@@ -301,7 +309,7 @@ constexpr int PIPE_STAGES = FX3D_PIPE_STAGES; // pairs in flight per thread: PIP
 inline uint32_t pipe_z_chunk(const GridDesc& g) { return g.Nz<(uint32_t)FX3D_PIPE_Z_CHUNK ? g.Nz : (uint32_t)FX3D_PIPE_Z_CHUNK; } // z planes per thread
 template<int Q, int ST> inline size_t pipe_smem(const int stages) { return (size_t)stages*pair_items<Q>()*BLOCK*2u*sizeof(typename Codec<ST>::T); }
 
-template<int Q, int ST, bool TRT, int EXT, int S> __global__ void __launch_bounds__(BLOCK, FX3D_PIPE_MIN_BLOCKS) k_stream_collide_pairs_pipe(const StepArgs a, const uint32_t zc) {
+template<int Q, int ST, bool TRT, int EXT, int S> __global__ void __launch_bounds__(BLOCK, ((EXT&EXT_SG)!=0 ? 2 : FX3D_PIPE_MIN_BLOCKS)) k_stream_collide_pairs_pipe(const StepArgs a, const uint32_t zc) {
 	typedef typename Codec<ST>::T T;
 	typedef typename PairStage<ST>::W SW;
 	constexpr bool EQ = (EXT&EXT_EQ)!=0, VF = (EXT&EXT_VF)!=0;
@@ -359,8 +367,8 @@ template<int Q, int ST, bool TRT, int EXT, int S> __global__ void __launch_bound
 			asm volatile("" ::: "memory");
 			read_pair<Q, ST>(w, f);
 		}
-		if(any_e) collide_v<Q, TRT, VF, ST, 2>(f, R, Rm1, ux, uy, uz, fx, fy, fz, is_e, a);
-		else collide_v<Q, TRT, VF, ST, 0>(f, R, Rm1, ux, uy, uz, fx, fy, fz, is_e, a);
+		if(any_e) collide_v<Q, TRT, VF, ST, 2, float2, Bool2, (EXT&EXT_SG)!=0>(f, R, Rm1, ux, uy, uz, fx, fy, fz, is_e, a);
+		else collide_v<Q, TRT, VF, ST, 0, float2, Bool2, (EXT&EXT_SG)!=0>(f, R, Rm1, ux, uy, uz, fx, fy, fz, is_e, a);
 		store_pair<Q, ST>((T*)a.fi, g.N, sa, sb, odd, f);
 	}
 }
@@ -547,7 +555,10 @@ template<int Q, int ST> __global__ void __launch_bounds__(BLOCK) k_update_force_
 inline dim3 cell_grid(const GridDesc& g) { return dim3((g.NxNy+BLOCK-1u)/BLOCK, g.Nz, 1u); }
 
 template<int ST, int Q, bool TRT, int EXT, bool FAST> inline cudaError_t sc_launch_t(const StepArgs& a, const int kind, cudaStream_t s) {
+	constexpr bool SG = (EXT&EXT_SG)!=0; // SUBGRID: one thread per cell or the prefetching two-cell kernel
 	if(kind==PATH_ROWS) {
+		if constexpr(SG) return cudaErrorInvalidConfiguration; // (the row kernel serves the adjoint, which has no SUBGRID)
+		else {
 		const RowPlan plan = row_plan(Q, ST, a.g.Nx, a.g.Ny, a.g.Nz);
 		if(plan.stages==0u) return cudaErrorInvalidConfiguration;
 		auto kernel = k_stream_collide_rows<Q, ST, TRT, EXT, FAST>;
@@ -560,11 +571,14 @@ template<int ST, int Q, bool TRT, int EXT, bool FAST> inline cudaError_t sc_laun
 		int grid = persistent_grid((const void*)kernel, tpb, plan.smem);
 		if((uint64_t)grid>rows_total) grid = (int)rows_total;
 		kernel<<<grid, tpb, plan.smem, s>>>(a, plan.stages);
+		}
 	} else if(kind==PATH_PAIRS||kind==PATH_PIPE) {
 		if constexpr(FAST) {
 			if(a.fi_dst!=a.fi||!pairs_supported(a.g)) return cudaErrorInvalidValue; // in place, even Nx, N < 2^32
-			if(kind==PATH_PAIRS) k_stream_collide_pairs<Q, ST, TRT, EXT><<<pair_grid(a.g), BLOCK, 0, s>>>(a);
-			else {
+			if(kind==PATH_PAIRS) {
+				if constexpr(SG) return cudaErrorInvalidConfiguration;
+				else k_stream_collide_pairs<Q, ST, TRT, EXT><<<pair_grid(a.g), BLOCK, 0, s>>>(a);
+			} else {
 				constexpr int S = PIPE_STAGES;
 				auto kernel = k_stream_collide_pairs_pipe<Q, ST, TRT, EXT, S>;
 				const size_t smem = pipe_smem<Q, ST>(S);
@@ -597,6 +611,28 @@ template<int ST, int Q, bool TRT> inline cudaError_t sc_ext(const int ext, const
 		default: return cudaErrorInvalidValue;
 	}
 }
+// SUBGRID variants: instantiated in lbm_kernels_<storage>_sg.cu (kind already resolved)
+template<int ST> cudaError_t launch_stream_collide_sg(const Variant& v, const StepArgs& a, int kind, cudaStream_t s);
+template<> cudaError_t launch_stream_collide_sg<ST_FP32>(const Variant& v, const StepArgs& a, int kind, cudaStream_t s);
+template<> cudaError_t launch_stream_collide_sg<ST_FP16S>(const Variant& v, const StepArgs& a, int kind, cudaStream_t s);
+template<> cudaError_t launch_stream_collide_sg<ST_FP16C>(const Variant& v, const StepArgs& a, int kind, cudaStream_t s);
+template<int ST, int Q, bool TRT> inline cudaError_t sc_ext_sg(const int ext, const StepArgs& a, const int kind, const bool fast, cudaStream_t s) {
+	switch(ext&~EXT_SG) {
+		case 0:                        return sc_launch<ST, Q, TRT, EXT_SG>(a, kind, fast, s);
+		case EXT_VF:                   return sc_launch<ST, Q, TRT, EXT_SG|EXT_VF>(a, kind, fast, s);
+		case EXT_VF|EXT_FF:            return sc_launch<ST, Q, TRT, EXT_SG|EXT_VF|EXT_FF>(a, kind, fast, s);
+		case EXT_EQ:                   return sc_launch<ST, Q, TRT, EXT_SG|EXT_EQ>(a, kind, fast, s);
+		case EXT_EQ|EXT_VF:            return sc_launch<ST, Q, TRT, EXT_SG|EXT_EQ|EXT_VF>(a, kind, fast, s);
+		case EXT_EQ|EXT_VF|EXT_FF:     return sc_launch<ST, Q, TRT, EXT_SG|EXT_EQ|EXT_VF|EXT_FF>(a, kind, fast, s);
+		default: return cudaErrorInvalidValue;
+	}
+}
+template<int ST> cudaError_t launch_stream_collide_sg_t(const Variant& v, const StepArgs& a, const int kind, cudaStream_t s) {
+	if(v.q==19) return v.trt ? sc_ext_sg<ST, 19, true>(v.ext, a, kind, v.fast, s) : sc_ext_sg<ST, 19, false>(v.ext, a, kind, v.fast, s);
+	if(v.q==27) return v.trt ? sc_ext_sg<ST, 27, true>(v.ext, a, kind, v.fast, s) : sc_ext_sg<ST, 27, false>(v.ext, a, kind, v.fast, s);
+	return cudaErrorInvalidValue;
+}
+
 template<int ST> cudaError_t launch_stream_collide_t(const Variant& v, const StepArgs& a, const int path, cudaStream_t s) {
 	// automatic choice (measured on 512x256x256): for fast arithmetic in place with 16-bit storage the
 	// two-cell kernel with per-thread prefetch; otherwise one thread per cell, in place or into another
@@ -607,6 +643,7 @@ template<int ST> cudaError_t launch_stream_collide_t(const Variant& v, const Ste
 	int kind = path;
 	if(path==PATH_AUTO) kind = pairs_ok && ST!=ST_FP32 ? PATH_PIPE : PATH_CELLS;
 	if((kind==PATH_ROWS && !rows_ok) || ((kind==PATH_PAIRS||kind==PATH_PIPE) && !pairs_ok)) return cudaErrorInvalidConfiguration;
+	if(v.ext&EXT_SG) return launch_stream_collide_sg<ST>(v, a, kind, s);
 	if(v.q==19) return v.trt ? sc_ext<ST, 19, true>(v.ext, a, kind, v.fast, s) : sc_ext<ST, 19, false>(v.ext, a, kind, v.fast, s);
 	if(v.q==27) return v.trt ? sc_ext<ST, 27, true>(v.ext, a, kind, v.fast, s) : sc_ext<ST, 27, false>(v.ext, a, kind, v.fast, s);
 	return cudaErrorInvalidValue;
@@ -628,7 +665,8 @@ template<int ST, int Q> inline bool uf_ext(const int ext, const StepArgs& a, con
 	}
 }
 template<int ST> cudaError_t launch_update_fields_t(const Variant& v, const StepArgs& a, cudaStream_t s) {
-	const bool ok = v.q==19 ? uf_ext<ST, 19>(v.ext, a, v.fast, s) : v.q==27 ? uf_ext<ST, 27>(v.ext, a, v.fast, s) : false;
+	const int ext = v.ext&~EXT_SG; // SUBGRID changes only the collision
+	const bool ok = v.q==19 ? uf_ext<ST, 19>(ext, a, v.fast, s) : v.q==27 ? uf_ext<ST, 27>(ext, a, v.fast, s) : false;
 	return ok ? cudaGetLastError() : cudaErrorInvalidValue;
 }
 
@@ -646,6 +684,11 @@ template<int ST> cudaError_t launch_update_force_field_t(const Variant& v, const
 }
 
 } // namespace fx3d
+
+#define FX3D_DEFINE_SG_LAUNCHER(ST) \
+	namespace fx3d { \
+	template<> cudaError_t launch_stream_collide_sg<ST>(const Variant& v, const StepArgs& a, const int kind, cudaStream_t s) { return launch_stream_collide_sg_t<ST>(v, a, kind, s); } \
+	}
 
 #define FX3D_DEFINE_LAUNCHERS(sfx, ST) \
 	namespace fx3d { \

@@ -208,6 +208,49 @@ template<bool VF> __device__ __forceinline__ void shift_clamp(float& ux, float& 
 
 // SRT / TRT collision of all directions in place (src/kernel.cpp:1595-1633). f: streamed DDFs,
 // rho/u: after force shift and clamp, fx..fz: total force, is_e: TYPE_E cell (f = feq).
+// ---------------------------------------------------------------- SUBGRID (src/kernel.cpp:1579-1593)
+// the collision rates of a cell from its relaxation rate w, with the reference's FP32 operations
+// (src/kernel.cpp:1598, 1606-1609; the host computes the same once for the uniform rate)
+__device__ __forceinline__ void cell_rates(const float w, float& omw, float& c_tau, float& hp, float& hm, float& c_taup, float& c_taum) {
+	const float wm = __fdiv_rn(1.0f, __fadd_rn(__fdiv_rn(0.1875f, __fsub_rn(__fdiv_rn(1.0f, w), 0.5f)), 0.5f));
+	omw = __fsub_rn(1.0f, w); c_tau = __fmaf_rn(w, -0.5f, 1.0f);
+	hp = __fmul_rn(0.5f, w); hm = __fmul_rn(0.5f, wm);
+	c_taup = __fmaf_rn(w, -0.25f, 0.5f); c_taum = __fmaf_rn(wm, -0.25f, 0.5f);
+}
+// Smagorinsky-Lilly: the relaxation rate of a cell from the non-equilibrium stress tensor
+// H = sum_i c_i c_i^T (f_i - feq_i) (components xx, yy, zz, xy, xz, yz) and its density:
+// w = 2/(tau0 + sqrt(tau0^2 + 0.76421222 sqrt(H:H)/rho)), tau0 = 1/w0, in the reference's order
+__device__ __forceinline__ float subgrid_w(const float w0, const float* H, const float rho) {
+	const float tau0 = __fdiv_rn(1.0f, w0);
+	const float diag = __fadd_rn(__fadd_rn(__fmul_rn(H[0], H[0]), __fmul_rn(H[1], H[1])), __fmul_rn(H[2], H[2]));
+	const float offd = __fadd_rn(__fadd_rn(__fmul_rn(H[3], H[3]), __fmul_rn(H[4], H[4])), __fmul_rn(H[5], H[5]));
+	const float Qs = __fadd_rn(diag, __fmul_rn(2.0f, offd));
+	return __fdiv_rn(2.0f, __fadd_rn(tau0, __fsqrt_rn(__fadd_rn(__fmul_rn(tau0, tau0), __fdiv_rn(__fmul_rn(0.76421222f, __fsqrt_rn(Qs)), rho)))));
+}
+// add the stress contribution v = f_i - feq_i of direction I (terms with a zero velocity component
+// are +-0 in the reference's sums and leave them unchanged, so they are skipped)
+template<int I> __device__ __forceinline__ void stress_add(float* H, const float v) {
+	constexpr int cx = vs_c(0, I), cy = vs_c(1, I), cz = vs_c(2, I);
+	if constexpr(cx!=0) H[0] = __fadd_rn(H[0], v);
+	if constexpr(cy!=0) H[1] = __fadd_rn(H[1], v);
+	if constexpr(cz!=0) H[2] = __fadd_rn(H[2], v);
+	if constexpr(cx!=0 && cy!=0) H[3] = __fadd_rn(H[3], cx*cy>0 ? v : -v);
+	if constexpr(cx!=0 && cz!=0) H[4] = __fadd_rn(H[4], cx*cz>0 ? v : -v);
+	if constexpr(cy!=0 && cz!=0) H[5] = __fadd_rn(H[5], cy*cz>0 ? v : -v);
+}
+// the subgrid relaxation rate from the streamed DDFs f and the equilibrium state (exact scheme)
+template<int Q> __device__ __forceinline__ float subgrid_w_exact(const float* f, const EqState& s, const float w0) {
+	float H[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+	Unroll<1, Q, 2>::run([&](auto ic) {
+		constexpr int i = decltype(ic)::value;
+		float fa, fb;
+		feq_pair<Q, i>(s, fa, fb);
+		stress_add<i>(H, __fsub_rn(f[i], fa));
+		stress_add<i+1>(H, __fsub_rn(f[i+1], fb));
+	});
+	return subgrid_w(w0, H, s.rho);
+}
+
 template<int Q, bool TRT, bool VF> __device__ __forceinline__ void collide(float* f, const float rho, const float ux, const float uy, const float uz,
                                                                           const float fx, const float fy, const float fz, const bool is_e, const StepArgs& a) {
 	const float w = a.w;

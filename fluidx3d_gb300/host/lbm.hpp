@@ -4,7 +4,7 @@
 //
 // The variant is chosen the way the reference chooses it, with macros defined before this header
 // is included (src/defines.hpp:5-29): D3Q19 (default) or D3Q27; SRT (default) or TRT; FP16S or
-// FP16C DDF storage (default FP32); VOLUME_FORCE, FORCE_FIELD, EQUILIBRIUM_BOUNDARIES; and, new here,
+// FP16C DDF storage (default FP32); VOLUME_FORCE, FORCE_FIELD, EQUILIBRIUM_BOUNDARIES, SUBGRID; and, new here,
 // EXACT_ARITHMETIC / FAST_ARITHMETIC (default: exact with FP32 storage, fast with FP16S/FP16C).
 //
 // Errors: the reference prints and exits (src/utilities.hpp:4159-4166); here a failed call throws
@@ -134,6 +134,9 @@ inline lbm_config lbm_config_from_defines(const uint Nx, const uint Ny, const ui
 #endif
 #if defined(EQUILIBRIUM_BOUNDARIES)
 	c.extensions |= LBM_EXT_EQUILIBRIUM_BOUNDARIES;
+#endif
+#if defined(SUBGRID)
+	c.extensions |= LBM_EXT_SUBGRID;
 #endif
 	c.device = -1;
 	c.nu = nu; c.fx = fx; c.fy = fy; c.fz = fz;

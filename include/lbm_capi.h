@@ -45,7 +45,8 @@ enum { LBM_FP32 = 0, LBM_FP16S = 1, LBM_FP16C = 2 };
 enum {
 	LBM_EXT_VOLUME_FORCE = 1,          /* VOLUME_FORCE: global force (fx,fy,fz), Guo forcing */
 	LBM_EXT_FORCE_FIELD = 2,           /* FORCE_FIELD: per-cell force F added to (fx,fy,fz) */
-	LBM_EXT_EQUILIBRIUM_BOUNDARIES = 4 /* EQUILIBRIUM_BOUNDARIES: TYPE_E cells held at their rho/u */
+	LBM_EXT_EQUILIBRIUM_BOUNDARIES = 4, /* EQUILIBRIUM_BOUNDARIES: TYPE_E cells held at their rho/u */
+	LBM_EXT_SUBGRID = 8                /* SUBGRID: Smagorinsky-Lilly relaxation rate per cell (src/kernel.cpp:1579-1593); not with lbm_run_adjoint */
 };
 /* arithmetic of the collision. EXACT evaluates the reference's FP32 operation order with IEEE
  * rounding at every step: bit-identical to the reference's kernel text evaluated on a CPU. FAST

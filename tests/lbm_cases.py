@@ -61,6 +61,9 @@ CASES = [
     Case("d3q27_srt_fp32_tgv", 27, "srt", "fp32"),
     Case("d3q27_trt_fp32_channel_eq_ff_vf", 27, "trt", "fp32", ("eq", "ff", "vf"), "channel", fx=1e-5),
     Case("d3q27_srt_fp16s_tgv", 27, "srt", "fp16s"),
+    Case("d3q19_srt_fp32_tgv_sg", 19, "srt", "fp32", ("sg",)),
+    Case("d3q19_trt_fp16s_channel_eq_sg", 19, "trt", "fp16s", ("eq", "sg"), "channel"),
+    Case("d3q27_trt_fp32_channel_eq_ff_sg_vf", 27, "trt", "fp32", ("eq", "ff", "sg", "vf"), "channel", fx=1e-5),
 ]
 CASE_BY_NAME = {c.name: c for c in CASES}
 

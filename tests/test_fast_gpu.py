@@ -37,6 +37,13 @@ def errors(lbm, o):
     return drho, du
 
 
+def skip_unsupported_path(case, path):
+    """SUBGRID runs on the one-cell and the prefetching two-cell kernels only (the row-staged kernel
+    serves the adjoint, which has no SUBGRID)."""
+    if "sg" in case.extensions and path in ("rows", "pairs"):
+        pytest.skip("no SUBGRID variant of this path")
+
+
 @pytest.fixture(params=["rows", "cells", "pairs", "pipe"])
 def path(request, monkeypatch):
     monkeypatch.setenv("FX3D_STREAM_COLLIDE_PATH", request.param)
@@ -59,6 +66,7 @@ def err_vs(rho, u, o):
 
 @pytest.mark.parametrize("case", LC.CASES, ids=[c.name for c in LC.CASES])
 def test_fast_within_tolerance_of_exact(case, gpu, path):
+    skip_unsupported_path(case, path)
     o = make_oracle(case)
     o.initialize()
     o.run(case.steps, *case.force)
@@ -114,12 +122,13 @@ def test_fast_force_reduction_close_to_exact(gpu):
 @pytest.mark.parametrize("case", LC.CASES + [LC.TGV64], ids=[c.name for c in LC.CASES] + [LC.TGV64.name])
 def test_pairs_bit_identical_to_one_cell_kernel(case, gpu, monkeypatch):
     out = {}
-    for p in ("cells", "pairs", "pipe"):
+    paths = ("cells", "pipe") if "sg" in case.extensions else ("cells", "pairs", "pipe")
+    for p in paths:
         monkeypatch.setenv("FX3D_STREAM_COLLIDE_PATH", p)
         with make_gpu(case, arithmetic="fast") as lbm:
             lbm.run(case.steps if case.steps < 200 else 200)
             out[p] = lbm.read_ddfs()
-    for p in ("pairs", "pipe"):
+    for p in paths[1:]:
         assert np.array_equal(out["cells"], out[p]), p
 
 
@@ -153,3 +162,18 @@ def test_pairs_need_even_nx(gpu, monkeypatch):
         with LBM(15, 8, 6, 0.05, storage="fp16s") as b:
             b.run(3)
             assert np.array_equal(a.read_ddfs(), b.read_ddfs())
+
+
+def test_subgrid_changes_the_flow_and_rejects_the_adjoint(gpu):
+    from fluidx3d_gb300 import LBMError
+    case = LC.CASE_BY_NAME["d3q19_trt_fp16s_channel_eq_sg"]
+    plain = LC.Case("plain", 19, "trt", "fp16s", ("eq",), "channel")
+    with make_gpu(case, arithmetic="fast") as a, make_gpu(plain, arithmetic="fast") as b:
+        a.run(case.steps)
+        b.run(case.steps)
+        assert not np.array_equal(a.read_ddfs(), b.read_ddfs())
+    sg = LC.Case("sg_adjoint", 19, "srt", "fp32", ("eq", "ff", "sg", "vf"), "channel")
+    with make_gpu(sg) as lbm:
+        with pytest.raises(LBMError) as e:
+            lbm.run_adjoint(4, "drag_x", window=(2, 4), marker=0x41, checkpoint_interval=2)
+        assert e.value.status == 5
