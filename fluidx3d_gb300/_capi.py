@@ -11,10 +11,10 @@ import os
 from . import build as _build
 
 LBM_OK = 0
-STATUS_NAMES = {1: "INVALID_ARGUMENT", 2: "OUT_OF_MEMORY", 3: "CUDA", 4: "NOT_INITIALIZED", 5: "UNSUPPORTED", 6: "NO_DEVICE"}
+STATUS_NAMES = {1: "INVALID_ARGUMENT", 2: "OUT_OF_MEMORY", 3: "CUDA", 4: "NOT_INITIALIZED", 5: "UNSUPPORTED", 6: "NO_DEVICE", 7: "IO"}
 SRT, TRT = 0, 1
 FP32, FP16S, FP16C = 0, 1, 2
-EXT_VOLUME_FORCE, EXT_FORCE_FIELD, EXT_EQUILIBRIUM_BOUNDARIES, EXT_SUBGRID = 1, 2, 4, 8
+EXT_VOLUME_FORCE, EXT_FORCE_FIELD, EXT_EQUILIBRIUM_BOUNDARIES, EXT_SUBGRID, EXT_MOVING_BOUNDARIES = 1, 2, 4, 8, 16
 FIELD_RHO, FIELD_U, FIELD_FLAGS, FIELD_F, FIELD_FI = 0, 1, 2, 3, 4
 ARITH_AUTO, ARITH_EXACT, ARITH_FAST = 0, 1, 2
 ARITHMETICS = {"auto": ARITH_AUTO, "exact": ARITH_EXACT, "fast": ARITH_FAST}
@@ -22,7 +22,8 @@ ARITHMETICS = {"auto": ARITH_AUTO, "exact": ARITH_EXACT, "fast": ARITH_FAST}
 COLLISIONS = {"srt": SRT, "trt": TRT}
 STORAGES = {"fp32": FP32, "fp16s": FP16S, "fp16c": FP16C}
 EXTENSIONS = {"volume_force": EXT_VOLUME_FORCE, "force_field": EXT_FORCE_FIELD, "equilibrium_boundaries": EXT_EQUILIBRIUM_BOUNDARIES,
-              "subgrid": EXT_SUBGRID, "vf": EXT_VOLUME_FORCE, "ff": EXT_FORCE_FIELD, "eq": EXT_EQUILIBRIUM_BOUNDARIES, "sg": EXT_SUBGRID}
+              "subgrid": EXT_SUBGRID, "moving_boundaries": EXT_MOVING_BOUNDARIES, "vf": EXT_VOLUME_FORCE, "ff": EXT_FORCE_FIELD,
+              "eq": EXT_EQUILIBRIUM_BOUNDARIES, "sg": EXT_SUBGRID, "mb": EXT_MOVING_BOUNDARIES}
 
 
 class LBMError(RuntimeError):
@@ -78,6 +79,8 @@ SIGNATURES = {
     "lbm_reset": ([_v], _i),
     "lbm_update_force_field": ([_v], _i),
     "lbm_reset_force_field": ([_v], _i),
+    "lbm_update_moving_boundaries": ([_v], _i),
+    "lbm_write_vtk": ([_v, _i, ctypes.c_char_p, _f, _f], _i),
     "lbm_object_center_of_mass": ([_v, _u8, ctypes.POINTER(_d)], _i),
     "lbm_object_force": ([_v, _u8, ctypes.POINTER(_d)], _i),
     "lbm_object_torque": ([_v, _u8, _d, _d, _d, ctypes.POINTER(_d)], _i),

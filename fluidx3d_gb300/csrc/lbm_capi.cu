@@ -8,6 +8,8 @@
 #include <cstring>
 #include <string>
 #include <new>
+#include <filesystem>
+#include <system_error>
 #include "lbm_capi.h"
 #include "lbm_internal.h"
 #include "lbm_adjoint.h"
@@ -250,6 +252,7 @@ uint32_t lbm_bandwidth_bytes_per_cell(const lbm_config* c) {
 	if(!c) return 0u;
 	uint32_t b = c->velocity_set*2u*(uint32_t)ddf_bytes(c->storage)+1u;
 	if(c->extensions&LBM_EXT_FORCE_FIELD) b += 12u;
+	if(c->extensions&LBM_EXT_MOVING_BOUNDARIES) b += c->velocity_set-1u; // neighbour flags (src/lbm.cpp:62-64)
 	return b;
 }
 
@@ -263,7 +266,7 @@ int lbm_domain_create(const lbm_config* c, lbm_domain** out) {
 	if(c->velocity_set!=19u&&c->velocity_set!=27u) return fail(LBM_ERR_INVALID_ARGUMENT, "velocity_set must be 19 or 27, got %u", c->velocity_set);
 	if(c->collision>LBM_TRT) return fail(LBM_ERR_INVALID_ARGUMENT, "collision must be LBM_SRT or LBM_TRT");
 	if(c->storage>LBM_FP16C) return fail(LBM_ERR_INVALID_ARGUMENT, "storage must be LBM_FP32, LBM_FP16S or LBM_FP16C");
-	if(c->extensions&~15u) return fail(LBM_ERR_INVALID_ARGUMENT, "unknown extension bits 0x%x", c->extensions&~15u);
+	if(c->extensions&~31u) return fail(LBM_ERR_INVALID_ARGUMENT, "unknown extension bits 0x%x", c->extensions&~31u);
 	if(c->arithmetic>LBM_ARITH_FAST) return fail(LBM_ERR_INVALID_ARGUMENT, "arithmetic must be LBM_ARITH_AUTO, LBM_ARITH_EXACT or LBM_ARITH_FAST");
 	if(!(c->nu>0.0f)) return fail(LBM_ERR_INVALID_ARGUMENT, c->nu==0.0f ? "Viscosity cannot be 0." : "Viscosity cannot be negative.");
 	if(!(c->extensions&LBM_EXT_VOLUME_FORCE)&&(c->fx!=0.0f||c->fy!=0.0f||c->fz!=0.0f))
@@ -294,6 +297,7 @@ int lbm_domain_create(const lbm_config* c, lbm_domain** out) {
 	if((c->extensions&LBM_EXT_FORCE_FIELD)&&(c->extensions&LBM_EXT_VOLUME_FORCE)) ext |= EXT_FF; // F acts on the fluid only with VOLUME_FORCE
 	if(c->extensions&LBM_EXT_EQUILIBRIUM_BOUNDARIES) ext |= EXT_EQ;
 	if(c->extensions&LBM_EXT_SUBGRID) ext |= EXT_SG;
+	if(c->extensions&LBM_EXT_MOVING_BOUNDARIES) ext |= EXT_MB;
 	d->v.ext = ext;
 	d->v.fast = c->arithmetic==LBM_ARITH_FAST || (c->arithmetic==LBM_ARITH_AUTO && c->storage!=LBM_FP32);
 	d->g.Nx = c->Nx; d->g.Ny = c->Ny; d->g.Nz = c->Nz; d->g.NxNy = c->Nx*c->Ny; d->g.N = N;
@@ -538,9 +542,109 @@ int lbm_voxelize_mesh(lbm_domain* d, const float* p0, const float* p1, const flo
 	if(e==cudaSuccess) e = cudaMemcpyAsync((char*)dev+3u*tb, bbu, sizeof(bbu), cudaMemcpyHostToDevice, d->stream);
 	if(e==cudaSuccess) e = launch_voxelize(d->v, d->g, direction, d->fi, d->u, d->flags, d->t+1ull, flag,
 	                                       dev, (const float*)((char*)dev+tb), (const float*)((char*)dev+2u*tb), (const float*)((char*)dev+3u*tb), d->stream);
+	// a moving solid marks its fluid neighbours (src/lbm.cpp:1082-1084)
+	const bool moving = sqrtf(lv[0]*lv[0]+lv[1]*lv[1]+lv[2]*lv[2])>0.0f || sqrtf(rv[0]*rv[0]+rv[1]*rv[1]+rv[2]*rv[2])>0.0f;
+	if(e==cudaSuccess && (d->v.ext&EXT_MB) && (flag&0x03u)==0x01u && moving) // (flag&(TYPE_S|TYPE_E))==TYPE_S
+		e = launch_update_moving_boundaries(d->v.q, d->g, d->u, d->flags, d->stream);
 	if(e==cudaSuccess) e = cudaStreamSynchronize(d->stream);
 	cudaFree(dev);
 	if(e!=cudaSuccess) return cuda_fail(e, "voxelize_mesh");
+	return LBM_OK;
+}
+
+// ---- VTK export
+namespace {
+struct VtkStaging { // two device + two pinned host chunks, freed on scope exit
+	void* dev[2] = {nullptr, nullptr};
+	void* host[2] = {nullptr, nullptr};
+	cudaEvent_t done[2] = {nullptr, nullptr};
+	std::FILE* file = nullptr;
+	~VtkStaging() {
+		for(int i=0; i<2; i++) {
+			if(dev[i]) cudaFree(dev[i]);
+			if(host[i]) cudaFreeHost(host[i]);
+			if(done[i]) cudaEventDestroy(done[i]);
+		}
+		if(file) std::fclose(file);
+	}
+};
+} // namespace
+
+int lbm_write_vtk(lbm_domain* d, const int field, const char* filename, const float spacing, const float scale) {
+	FX3D_DOMAIN(d);
+	if(!filename||!*filename) return fail(LBM_ERR_INVALID_ARGUMENT, "lbm_write_vtk: no file name");
+	if(field!=LBM_FIELD_RHO&&field!=LBM_FIELD_U&&field!=LBM_FIELD_FLAGS&&field!=LBM_FIELD_F)
+		return fail(LBM_ERR_INVALID_ARGUMENT, "lbm_write_vtk: field %d has no VTK form (rho, u, flags or F)", field);
+	if(field==LBM_FIELD_F && !d->F) return fail(LBM_ERR_UNSUPPORTED, "F does not exist: enable LBM_EXT_FORCE_FIELD or call lbm_update_force_field");
+	if(d->initialized && (field==LBM_FIELD_RHO||field==LBM_FIELD_U)) { const int r = do_update_fields(d); if(r!=LBM_OK) return r; }
+	const uint32_t dims = field==LBM_FIELD_U||field==LBM_FIELD_F ? 3u : 1u;
+	const bool u8 = field==LBM_FIELD_FLAGS;
+	const size_t elem = u8 ? 1u : 4u;
+	// header of src/lbm.hpp:308-317: title "FluidX3D <file name>", origin at the box centre, numbers as std::to_string
+	const std::string path(filename);
+	const size_t slash = path.rfind('/');
+	const std::string base = slash==std::string::npos ? path : path.substr(slash+1u);
+	const float ox = spacing*(0.5f-0.5f*(float)d->g.Nx), oy = spacing*(0.5f-0.5f*(float)d->g.Ny), oz = spacing*(0.5f-0.5f*(float)d->g.Nz);
+	char head[1024];
+	const int hl = std::snprintf(head, sizeof(head),
+		"# vtk DataFile Version 3.0\nFluidX3D %s\nBINARY\nDATASET STRUCTURED_POINTS\nDIMENSIONS %u %u %u\nORIGIN %f %f %f\nSPACING %f %f %f\n"
+		"POINT_DATA %llu\nSCALARS data %s %u\nLOOKUP_TABLE default\n",
+		base.c_str(), d->g.Nx, d->g.Ny, d->g.Nz, (double)ox, (double)oy, (double)oz, (double)spacing, (double)spacing, (double)spacing,
+		(unsigned long long)d->g.N, u8 ? "unsigned_char" : "float", dims);
+	if(hl<=0||hl>=(int)sizeof(head)) return fail(LBM_ERR_INVALID_ARGUMENT, "lbm_write_vtk: file name too long");
+	if(slash!=std::string::npos && slash>0u) { // create the folder like the reference's create_folder (src/utilities.hpp:4197-4204)
+		std::error_code ec;
+		std::filesystem::create_directories(path.substr(0u, slash), ec);
+	}
+	VtkStaging st;
+	st.file = std::fopen(filename, "wb");
+	if(!st.file) return fail(LBM_ERR_IO, "lbm_write_vtk: cannot open \"%s\" for writing", filename);
+	if(std::fwrite(head, 1u, (size_t)hl, st.file)!=(size_t)hl) return fail(LBM_ERR_IO, "lbm_write_vtk: write to \"%s\" failed", filename);
+	// chunks of up to 16M values, packed on the GPU (FP32 fields) while the previous chunk is written
+	uint64_t chunk_cells = (16ull<<20)/dims;
+	if(chunk_cells>d->g.N) chunk_cells = d->g.N;
+	const size_t chunk_bytes = (size_t)chunk_cells*dims*elem;
+	for(int i=0; i<2; i++) {
+		if(!u8) FX3D_CUDA(cudaMalloc(&st.dev[i], chunk_bytes), "cudaMalloc(vtk staging)");
+		FX3D_CUDA(cudaHostAlloc(&st.host[i], chunk_bytes, cudaHostAllocDefault), "cudaHostAlloc(vtk staging)");
+		FX3D_CUDA(cudaEventCreateWithFlags(&st.done[i], cudaEventDisableTiming), "cudaEventCreate");
+	}
+	const uint64_t chunks = (d->g.N+chunk_cells-1ull)/chunk_cells;
+	const float* src = (const float*)d->field_ptr(field);
+	auto issue = [&](const uint64_t k) -> cudaError_t {
+		const int b = (int)(k&1ull);
+		const uint64_t first = k*chunk_cells, count = first+chunk_cells<=d->g.N ? chunk_cells : d->g.N-first;
+		cudaError_t e;
+		if(u8) e = cudaMemcpyAsync(st.host[b], d->flags+first, (size_t)count, cudaMemcpyDeviceToHost, d->stream);
+		else {
+			e = launch_pack_vtk(src, d->g.N, dims, first, count, scale, (uint32_t*)st.dev[b], d->stream);
+			if(e==cudaSuccess) e = cudaMemcpyAsync(st.host[b], st.dev[b], (size_t)count*dims*4u, cudaMemcpyDeviceToHost, d->stream);
+		}
+		if(e==cudaSuccess) e = cudaEventRecord(st.done[b], d->stream);
+		return e;
+	};
+	FX3D_CUDA(issue(0ull), "vtk chunk");
+	for(uint64_t k=0ull; k<chunks; k++) {
+		if(k+1ull<chunks) FX3D_CUDA(issue(k+1ull), "vtk chunk"); // the buffers of chunk k-1, written out already
+		const int b = (int)(k&1ull);
+		FX3D_CUDA(cudaEventSynchronize(st.done[b]), "cudaEventSynchronize");
+		const uint64_t first = k*chunk_cells, count = first+chunk_cells<=d->g.N ? chunk_cells : d->g.N-first;
+		const size_t nb = (size_t)count*dims*elem;
+		if(std::fwrite(st.host[b], 1u, nb, st.file)!=nb) {
+			cudaStreamSynchronize(d->stream);
+			return fail(LBM_ERR_IO, "lbm_write_vtk: write to \"%s\" failed", filename);
+		}
+	}
+	const int rc = std::fclose(st.file);
+	st.file = nullptr;
+	if(rc!=0) return fail(LBM_ERR_IO, "lbm_write_vtk: closing \"%s\" failed", filename);
+	return LBM_OK;
+}
+
+int lbm_update_moving_boundaries(lbm_domain* d) {
+	FX3D_DOMAIN(d);
+	if(!(d->v.ext&EXT_MB)) return fail(LBM_ERR_UNSUPPORTED, "lbm_update_moving_boundaries needs LBM_EXT_MOVING_BOUNDARIES");
+	FX3D_CUDA(launch_update_moving_boundaries(d->v.q, d->g, d->u, d->flags, d->stream), "update_moving_boundaries");
 	return LBM_OK;
 }
 
@@ -600,6 +704,7 @@ extern "C" int lbm_run_adjoint(lbm_domain* d, const lbm_adjoint_config* cfg, dou
 	if(!cfg) return fail(LBM_ERR_INVALID_ARGUMENT, "lbm_run_adjoint: NULL config");
 	if(!d->initialized) return fail(LBM_ERR_NOT_INITIALIZED, "lbm_run_adjoint: call lbm_initialize first");
 	if(d->v.ext&EXT_SG) return fail(LBM_ERR_UNSUPPORTED, "lbm_run_adjoint does not support LBM_EXT_SUBGRID (the adjoint has no Smagorinsky-Lilly term)");
+	if(d->v.ext&EXT_MB) return fail(LBM_ERR_UNSUPPORTED, "lbm_run_adjoint does not support LBM_EXT_MOVING_BOUNDARIES");
 	if(!adjoint_supported(d->v) || !d->F) return fail(LBM_ERR_UNSUPPORTED, "lbm_run_adjoint needs LBM_EXT_VOLUME_FORCE and LBM_EXT_FORCE_FIELD (F is the design variable)");
 	if(d->g.N>0xFFFFFFFFull) return fail(LBM_ERR_UNSUPPORTED, "lbm_run_adjoint needs fewer than 2^32 cells (its kernels use 32-bit cell indices)");
 	if(cfg->steps==0ull||cfg->checkpoint_interval==0ull) return fail(LBM_ERR_INVALID_ARGUMENT, "lbm_run_adjoint: steps and checkpoint_interval must be >= 1");

@@ -2,6 +2,8 @@
 //
 //   k_object_sum + k_object_sum_final  src/kernel.cpp:1901-1959 object_center_of_mass/force/torque
 //   k_unvoxelize                       src/kernel.cpp:2359-2363 unvoxelize_mesh
+//   k_update_moving_boundaries         src/kernel.cpp:1431-1450 update_moving_boundaries
+//   k_pack_vtk                         src/lbm.hpp:298-340 write_vtk (unit scaling, AoS, big-endian)
 //
 // The reference reduces 64-cell work-groups in local memory and adds the group sums into 4 floats
 // with float atomics, so its result depends on scheduling. Here each of REDUCE_BLOCKS blocks
@@ -137,6 +139,59 @@ __global__ void __launch_bounds__(BLOCK) k_unvoxelize(const GridDesc g, uint8_t*
 cudaError_t launch_unvoxelize(const GridDesc& g, uint8_t* flags, const uint8_t flag, const float* box, cudaStream_t s) {
 	const dim3 grid((g.NxNy+BLOCK-1u)/BLOCK, g.Nz, 1u);
 	k_unvoxelize<<<grid, BLOCK, 0, s>>>(g, flags, flag, box[0], box[1], box[2], box[3], box[4], box[5]);
+	return cudaGetLastError();
+}
+
+// TYPE_MS set on cells (not TYPE_S, TYPE_E or TYPE_T) with a TYPE_S neighbour whose velocity is not
+// zero, cleared on the others. A neighbour's flags are read only through the TYPE_S test, whose bit
+// pattern the marking never produces or removes (00 <-> 11): the result is independent of the order
+// in which the cells are marked.
+template<int Q> __global__ void __launch_bounds__(BLOCK) k_update_moving_boundaries(const GridDesc gd, const float* __restrict__ u, uint8_t* flags) {
+	const Grid& g = reinterpret_cast<const Grid&>(gd);
+	const uint32_t xy = blockIdx.x*(uint32_t)BLOCK+threadIdx.x;
+	if(xy>=g.NxNy) return;
+	const uint32_t z = blockIdx.y, y = div_nx(g, xy), x = xy-y*g.Nx;
+	const uint64_t n = (uint64_t)z*g.NxNy+xy, N = g.N;
+	const uint8_t flagsn = flags[n], flagsn_bo = flagsn&TYPE_BO;
+	if(flagsn_bo==TYPE_S||flagsn_bo==TYPE_E||(flagsn&TYPE_T)) return;
+	const Nbr nb(g, x, y, z);
+	bool next = false;
+	Unroll<1, Q, 1>::run([&](auto ic) {
+		const uint64_t j = nb.template j<decltype(ic)::value>();
+		next = next||((flags[j]&TYPE_BO)==TYPE_S&&(u[j]!=0.0f||u[N+j]!=0.0f||u[2ull*N+j]!=0.0f));
+	});
+	flags[n] = next ? (uint8_t)(flagsn|TYPE_MS) : (uint8_t)(flagsn&~TYPE_MS);
+}
+
+// VTK export: values [first, first+count) of a field of `dims` FP32 components stored in SoA blocks
+// of N, each multiplied by `scale` (the reference's unit conversion, one FP32 multiply), written
+// interleaved per cell (x,y,z) and byte-reversed to big-endian, as the legacy VTK binary format wants
+__global__ void __launch_bounds__(BLOCK) k_pack_vtk(const float* __restrict__ src, const uint64_t N, const uint32_t dims, const uint64_t first,
+                                                    const uint64_t count, const float scale, uint32_t* __restrict__ dst) {
+	const uint64_t total = count*dims;
+	for(uint64_t k=(uint64_t)blockIdx.x*BLOCK+threadIdx.x; k<total; k+=(uint64_t)gridDim.x*BLOCK) {
+		const uint64_t i = k/dims;
+		const uint32_t c = (uint32_t)(k-i*dims);
+		const float v = __fmul_rn(scale, src[(uint64_t)c*N+first+i]);
+		dst[k] = __byte_perm(__float_as_uint(v), 0u, 0x0123u);
+	}
+}
+
+cudaError_t launch_pack_vtk(const float* src, const uint64_t N, const uint32_t dims, const uint64_t first, const uint64_t count, const float scale,
+                            uint32_t* dst, cudaStream_t s) {
+	const uint64_t total = count*dims;
+	if(total==0ull) return cudaSuccess;
+	const uint64_t blocks = (total+BLOCK-1u)/BLOCK;
+	k_pack_vtk<<<(unsigned)(blocks<4864ull ? blocks : 4864ull), BLOCK, 0, s>>>(src, N, dims, first, count, scale, dst); // 152 SMs x 32
+	return cudaGetLastError();
+}
+
+cudaError_t launch_update_moving_boundaries(const int q, const GridDesc& g, const float* u, uint8_t* flags, cudaStream_t s) {
+	static_assert(sizeof(GridDesc)==sizeof(Grid), "GridDesc must mirror Grid");
+	const dim3 grid((g.NxNy+BLOCK-1u)/BLOCK, g.Nz, 1u);
+	if(q==19) k_update_moving_boundaries<19><<<grid, BLOCK, 0, s>>>(g, u, flags);
+	else if(q==27) k_update_moving_boundaries<27><<<grid, BLOCK, 0, s>>>(g, u, flags);
+	else return cudaErrorInvalidValue;
 	return cudaGetLastError();
 }
 

@@ -6,7 +6,7 @@
 namespace fx3d {
 
 enum : int { ST_FP32 = 0, ST_FP16S = 1, ST_FP16C = 2 }; // DDF storage formats
-enum : int { EXT_VF = 1, EXT_FF = 2, EXT_EQ = 4, EXT_SG = 8 }; // VOLUME_FORCE, FORCE_FIELD, EQUILIBRIUM_BOUNDARIES, SUBGRID
+enum : int { EXT_VF = 1, EXT_FF = 2, EXT_EQ = 4, EXT_SG = 8, EXT_MB = 16 }; // VOLUME_FORCE, FORCE_FIELD, EQUILIBRIUM_BOUNDARIES, SUBGRID, MOVING_BOUNDARIES
 
 struct GridDesc { // mirrors fx3d::Grid of lbm_scheme.cuh (kept layout-identical)
 	uint32_t Nx, Ny, Nz, NxNy;
@@ -83,6 +83,10 @@ cudaError_t launch_object_sum_blocks(const GridDesc& g, const float* F, const ui
 int capi_fail(int code, const char* message);
 int capi_cuda_fail(cudaError_t e, const char* what);
 cudaError_t launch_unvoxelize(const GridDesc& g, uint8_t* flags, uint8_t flag, const float* box, cudaStream_t s);
+// VTK export packing: count cells from `first` of a dims-component FP32 SoA field, scaled, AoS, big-endian
+cudaError_t launch_pack_vtk(const float* src, uint64_t N, uint32_t dims, uint64_t first, uint64_t count, float scale, uint32_t* dst, cudaStream_t s);
+// TYPE_MS marking of the cells next to moving solids (src/kernel.cpp:1431-1450)
+cudaError_t launch_update_moving_boundaries(int q, const GridDesc& g, const float* u, uint8_t* flags, cudaStream_t s);
 
 // voxelization (lbm_voxelize.cu); bbu: 16 floats in the reference's layout (src/lbm.cpp:280-296)
 cudaError_t launch_voxelize(const Variant& v, const GridDesc& g, uint32_t direction, void* fi, float* u, uint8_t* flags, uint64_t t, uint8_t flag,

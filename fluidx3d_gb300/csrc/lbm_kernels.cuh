@@ -8,6 +8,8 @@
 //   k_stream_collide_pairs  the same, two x-adjacent cells per thread (fast arithmetic)
 //   k_update_fields       src/kernel.cpp:1794-1870 update_fields
 //   k_update_force_field  src/kernel.cpp:1873-1884 update_force_field
+// MOVING_BOUNDARIES (EXT_MB) adds apply_moving_boundaries (src/kernel.cpp:1104-1113) to
+// stream_collide and update_fields and the TYPE_MS marking of initialize (src/kernel.cpp:1378-1387).
 #pragma once
 #include "lbm_scheme.cuh"
 #include "lbm_internal.h"
@@ -32,14 +34,37 @@ __device__ __forceinline__ bool cell_of_thread(const Grid& g, CellPos& c) {
 	return true;
 }
 
-template<int Q, int ST> __global__ void __launch_bounds__(BLOCK) k_initialize(const StepArgs a) {
+// true if a neighbour of the cell is a TYPE_S cell with u != 0 (src/kernel.cpp:1381-1385, 1441-1447)
+template<int Q, class J> __device__ __forceinline__ bool next_to_moving_boundary(const float* __restrict__ u, const uint8_t* flags, const uint64_t N, const J& nbr) {
+	bool next = false;
+	Unroll<1, Q, 1>::run([&](auto ic) {
+		const uint64_t j = nbr(ic);
+		next = next||((flags[j]&TYPE_BO)==TYPE_S&&(u[j]!=0.0f||u[N+j]!=0.0f||u[2ull*N+j]!=0.0f));
+	});
+	return next;
+}
+
+// mb: MOVING_BOUNDARIES, where solid cells keep their (wall) velocity unless all their neighbours are
+// solid, and the other cells but TYPE_E get TYPE_MS set or cleared. The flags a cell writes are read
+// by its neighbours only through the TYPE_S test, whose bit pattern the marking never produces or
+// removes (00 <-> 11), so the result does not depend on the order the cells run in.
+template<int Q, int ST> __global__ void __launch_bounds__(BLOCK) k_initialize(const StepArgs a, uint8_t* flags, const bool mb) {
 	typedef typename Codec<ST>::T T;
 	const Grid& g = grid_of(a.g);
 	CellPos c;
 	if(!cell_of_thread(g, c)) return;
 	const uint64_t n = c.n, N = g.N;
+	const Nbr nb(g, c.x, c.y, c.z);
+	const uint8_t flagsn = flags[n], flagsn_bo = flagsn&TYPE_BO;
 	float ux, uy, uz;
-	if((a.flags[n]&TYPE_BO)==TYPE_S) { // solid cells start at rest (src/kernel.cpp:1370-1373)
+	bool rest = flagsn_bo==TYPE_S; // solid cells start at rest (src/kernel.cpp:1370-1377)
+	if(mb && rest) {
+		Unroll<1, Q, 1>::run([&](auto ic) { rest = rest&&(flags[nb.template j<decltype(ic)::value>()]&TYPE_BO)==TYPE_S; });
+	} else if(mb && flagsn_bo!=TYPE_E) {
+		const bool next = next_to_moving_boundary<Q>(a.u, flags, N, [&](auto ic) { return nb.template j<decltype(ic)::value>(); });
+		flags[n] = next ? (uint8_t)(flagsn|TYPE_MS) : (uint8_t)(flagsn&~TYPE_MS);
+	}
+	if(rest) {
 		ux = uy = uz = 0.0f;
 		a.u[n] = 0.0f; a.u[N+n] = 0.0f; a.u[2ull*N+n] = 0.0f;
 	} else {
@@ -49,8 +74,24 @@ template<int Q, int ST> __global__ void __launch_bounds__(BLOCK) k_initialize(co
 	float f[Q];
 	f[0] = feq0<Q>(s);
 	Unroll<1, Q, 2>::run([&](auto ic) { constexpr int i = decltype(ic)::value; feq_pair<Q, i>(s, f[i], f[i+1]); });
-	const Nbr nb(g, c.x, c.y, c.z);
 	store_f<Q, ST>((T*)a.fi, N, n, nb, true, f); // odd parity (src/kernel.cpp:1429)
+}
+
+// Moving solid boundaries (src/kernel.cpp:1104-1113 apply_moving_boundaries) on the streamed DDFs of
+// a TYPE_MS cell, before its density and velocity are taken: population i (i odd) gains
+// -6 w_i (c_{i+1}.u_s) when the neighbour along c_{i+1} is a TYPE_S cell moving at u_s, population
+// i+1 gains -6 w_i (c_i.u_s) from the neighbour along c_i (wall density 1). nbr(integral_constant<I>)
+// is the neighbour index along c_I. f in real units (scale 1) or in storage units (scale K, a power
+// of two: fma(K w6, c.u, K f) is exactly K fma(w6, c.u, f), so both forms add the same correction).
+template<int Q, class J> __device__ __forceinline__ void apply_moving_boundaries(float* f, const StepArgs& a, const float scale, const J& nbr) {
+	const uint64_t N = a.g.N;
+	Unroll<1, Q, 2>::run([&](auto ic) {
+		constexpr int i = decltype(ic)::value;
+		const float w6 = __fmul_rn(__fmul_rn(-6.0f, vs_w<Q>(i)), scale);
+		const uint64_t jb = nbr(std::integral_constant<int, i+1>()), ja = nbr(std::integral_constant<int, i>());
+		if((a.flags[jb]&TYPE_BO)==TYPE_S) f[i] = __fmaf_rn(w6, cdot<i+1>(a.u[jb], a.u[N+jb], a.u[2ull*N+jb]), f[i]);
+		if((a.flags[ja]&TYPE_BO)==TYPE_S) f[i+1] = __fmaf_rn(w6, cdot<i>(a.u[ja], a.u[N+ja], a.u[2ull*N+ja]), f[i+1]);
+	});
 }
 
 // density and velocity of one cell from its streamed DDFs (or the preset TYPE_E values), force
@@ -125,6 +166,9 @@ template<int Q, int ST, bool TRT, int EXT, bool FAST> __global__ void __launch_b
 	const Nbr nb(g, c.x, c.y, c.z);
 	float f[Q];
 	load_f<Q, ST, StepCodec<ST, FAST>>((const T*)a.fi, g.N, n, nb, odd, f);
+	if constexpr((EXT&EXT_MB)!=0) {
+		if(flagsn_bo==TYPE_MS) apply_moving_boundaries<Q>(f, a, FAST ? RawCodec<ST>::K : 1.0f, [&](auto ic) { return nb.template j<decltype(ic)::value>(); });
+	}
 	const bool is_e = EQ && flagsn_bo==TYPE_E;
 	cell_step<Q, ST, TRT, EXT, FAST>(f, a, n, is_e);
 	store_f<Q, ST, StepCodec<ST, FAST>>((T*)a.fi_dst, g.N, n, nb, odd, f);
@@ -346,6 +390,25 @@ template<int Q, int ST, bool TRT, int EXT, int S> __global__ void __launch_bound
 		const uint32_t fa = fl&0xFFu, fb = (fl>>8)&0xFFu;
 		const bool skip_a = (fa&TYPE_BO)==TYPE_S||(fa&TYPE_SU)==TYPE_G, skip_b = (fb&TYPE_BO)==TYPE_S||(fb&TYPE_SU)==TYPE_G;
 		if(skip_a&&skip_b) continue;
+		if constexpr((EXT&EXT_MB)!=0) {
+			const bool ms_a = (fa&TYPE_BO)==TYPE_MS, ms_b = (fb&TYPE_BO)==TYPE_MS;
+			if(ms_a||ms_b) { // next to a moving solid: the pair's cells step one at a time (values read from the stage per cell)
+				#pragma unroll 1
+				for(uint32_t c=0u; c<2u; c++) {
+					if(c ? skip_b : skip_a) continue;
+					const Steps32 s(g, x+c, y, z, n+c);
+					float2 fp[Q];
+					read_pair<Q, ST>(w, fp);
+					float f1[Q];
+					#pragma unroll
+					for(int k=0; k<Q; k++) f1[k] = c ? fp[k].y : fp[k].x;
+					if(c ? ms_b : ms_a) apply_moving_boundaries<Q>(f1, a, RawCodec<ST>::K, [&](auto ic) { return (uint64_t)s.template j<decltype(ic)::value>(); });
+					cell_step<Q, ST, TRT, EXT, true>(f1, a, n+c, EQ && ((c ? fb : fa)&TYPE_BO)==TYPE_E);
+					store_f32<Q, RawCodec<ST>>((T*)a.fi, g.N, s, odd, f1);
+				}
+				continue;
+			}
+		}
 		float2 f[Q];
 		read_pair<Q, ST>(w, f);
 		if(skip_a||skip_b) { // one cell of the pair steps alone
@@ -509,7 +572,7 @@ k_stream_collide_rows(const StepArgs a, const uint32_t stages) {
 	if(copier) bulk_wait_all(); // stores complete before the CTA (and its shared memory) goes away
 }
 
-template<int Q, int ST, int EXT, bool FAST> __global__ void __launch_bounds__(BLOCK) k_update_fields(const StepArgs a) {
+template<int Q, int ST, int EXT, bool FAST> __global__ void __launch_bounds__(BLOCK) k_update_fields(const StepArgs a, const bool mb) {
 	typedef typename Codec<ST>::T T;
 	constexpr bool EQ = (EXT&EXT_EQ)!=0;
 	const Grid& g = grid_of(a.g);
@@ -523,6 +586,7 @@ template<int Q, int ST, int EXT, bool FAST> __global__ void __launch_bounds__(BL
 	const Nbr nb(g, c.x, c.y, c.z);
 	float f[Q];
 	load_f<Q, ST, StepCodec<ST, FAST>>((const T*)a.fi, N, n, nb, (a.t&1ull)!=0ull, f);
+	if(mb && flagsn_bo==TYPE_MS) apply_moving_boundaries<Q>(f, a, FAST ? RawCodec<ST>::K : 1.0f, [&](auto ic) { return nb.template j<decltype(ic)::value>(); });
 	float rho, ux, uy, uz, fx, fy, fz;
 	if constexpr(FAST) {
 		float rm1, inv;
@@ -555,9 +619,10 @@ template<int Q, int ST> __global__ void __launch_bounds__(BLOCK) k_update_force_
 inline dim3 cell_grid(const GridDesc& g) { return dim3((g.NxNy+BLOCK-1u)/BLOCK, g.Nz, 1u); }
 
 template<int ST, int Q, bool TRT, int EXT, bool FAST> inline cudaError_t sc_launch_t(const StepArgs& a, const int kind, cudaStream_t s) {
-	constexpr bool SG = (EXT&EXT_SG)!=0; // SUBGRID: one thread per cell or the prefetching two-cell kernel
+	// SUBGRID and MOVING_BOUNDARIES: one thread per cell or the prefetching two-cell kernel
+	constexpr bool SG = (EXT&(EXT_SG|EXT_MB))!=0;
 	if(kind==PATH_ROWS) {
-		if constexpr(SG) return cudaErrorInvalidConfiguration; // (the row kernel serves the adjoint, which has no SUBGRID)
+		if constexpr(SG) return cudaErrorInvalidConfiguration; // (the row kernel serves the adjoint, which has neither)
 		else {
 		const RowPlan plan = row_plan(Q, ST, a.g.Nx, a.g.Ny, a.g.Nz);
 		if(plan.stages==0u) return cudaErrorInvalidConfiguration;
@@ -611,25 +676,32 @@ template<int ST, int Q, bool TRT> inline cudaError_t sc_ext(const int ext, const
 		default: return cudaErrorInvalidValue;
 	}
 }
-// SUBGRID variants: instantiated in lbm_kernels_<storage>_sg.cu (kind already resolved)
-template<int ST> cudaError_t launch_stream_collide_sg(const Variant& v, const StepArgs& a, int kind, cudaStream_t s);
-template<> cudaError_t launch_stream_collide_sg<ST_FP32>(const Variant& v, const StepArgs& a, int kind, cudaStream_t s);
-template<> cudaError_t launch_stream_collide_sg<ST_FP16S>(const Variant& v, const StepArgs& a, int kind, cudaStream_t s);
-template<> cudaError_t launch_stream_collide_sg<ST_FP16C>(const Variant& v, const StepArgs& a, int kind, cudaStream_t s);
-template<int ST, int Q, bool TRT> inline cudaError_t sc_ext_sg(const int ext, const StepArgs& a, const int kind, const bool fast, cudaStream_t s) {
-	switch(ext&~EXT_SG) {
-		case 0:                        return sc_launch<ST, Q, TRT, EXT_SG>(a, kind, fast, s);
-		case EXT_VF:                   return sc_launch<ST, Q, TRT, EXT_SG|EXT_VF>(a, kind, fast, s);
-		case EXT_VF|EXT_FF:            return sc_launch<ST, Q, TRT, EXT_SG|EXT_VF|EXT_FF>(a, kind, fast, s);
-		case EXT_EQ:                   return sc_launch<ST, Q, TRT, EXT_SG|EXT_EQ>(a, kind, fast, s);
-		case EXT_EQ|EXT_VF:            return sc_launch<ST, Q, TRT, EXT_SG|EXT_EQ|EXT_VF>(a, kind, fast, s);
-		case EXT_EQ|EXT_VF|EXT_FF:     return sc_launch<ST, Q, TRT, EXT_SG|EXT_EQ|EXT_VF|EXT_FF>(a, kind, fast, s);
+// SUBGRID / MOVING_BOUNDARIES variants: instantiated in lbm_kernels_<storage>_<sg|mb|sgmb>.cu, one
+// translation unit per combination XB of the two bits (kind already resolved)
+template<int ST, int XB> cudaError_t launch_stream_collide_x(const Variant& v, const StepArgs& a, int kind, cudaStream_t s);
+#define FX3D_DECLARE_X_LAUNCHERS(ST) \
+	template<> cudaError_t launch_stream_collide_x<ST, EXT_SG>(const Variant& v, const StepArgs& a, int kind, cudaStream_t s); \
+	template<> cudaError_t launch_stream_collide_x<ST, EXT_MB>(const Variant& v, const StepArgs& a, int kind, cudaStream_t s); \
+	template<> cudaError_t launch_stream_collide_x<ST, EXT_SG|EXT_MB>(const Variant& v, const StepArgs& a, int kind, cudaStream_t s);
+FX3D_DECLARE_X_LAUNCHERS(ST_FP32)
+FX3D_DECLARE_X_LAUNCHERS(ST_FP16S)
+FX3D_DECLARE_X_LAUNCHERS(ST_FP16C)
+#undef FX3D_DECLARE_X_LAUNCHERS
+template<int ST, int Q, bool TRT, int XB> inline cudaError_t sc_ext_x(const int ext, const StepArgs& a, const int kind, const bool fast, cudaStream_t s) {
+	switch(ext&~(EXT_SG|EXT_MB)) {
+		case 0:                        return sc_launch<ST, Q, TRT, XB>(a, kind, fast, s);
+		case EXT_VF:                   return sc_launch<ST, Q, TRT, XB|EXT_VF>(a, kind, fast, s);
+		case EXT_VF|EXT_FF:            return sc_launch<ST, Q, TRT, XB|EXT_VF|EXT_FF>(a, kind, fast, s);
+		case EXT_EQ:                   return sc_launch<ST, Q, TRT, XB|EXT_EQ>(a, kind, fast, s);
+		case EXT_EQ|EXT_VF:            return sc_launch<ST, Q, TRT, XB|EXT_EQ|EXT_VF>(a, kind, fast, s);
+		case EXT_EQ|EXT_VF|EXT_FF:     return sc_launch<ST, Q, TRT, XB|EXT_EQ|EXT_VF|EXT_FF>(a, kind, fast, s);
 		default: return cudaErrorInvalidValue;
 	}
 }
-template<int ST> cudaError_t launch_stream_collide_sg_t(const Variant& v, const StepArgs& a, const int kind, cudaStream_t s) {
-	if(v.q==19) return v.trt ? sc_ext_sg<ST, 19, true>(v.ext, a, kind, v.fast, s) : sc_ext_sg<ST, 19, false>(v.ext, a, kind, v.fast, s);
-	if(v.q==27) return v.trt ? sc_ext_sg<ST, 27, true>(v.ext, a, kind, v.fast, s) : sc_ext_sg<ST, 27, false>(v.ext, a, kind, v.fast, s);
+template<int ST, int XB> cudaError_t launch_stream_collide_x_t(const Variant& v, const StepArgs& a, const int kind, cudaStream_t s) {
+	if((v.ext&(EXT_SG|EXT_MB))!=XB) return cudaErrorInvalidValue;
+	if(v.q==19) return v.trt ? sc_ext_x<ST, 19, true, XB>(v.ext, a, kind, v.fast, s) : sc_ext_x<ST, 19, false, XB>(v.ext, a, kind, v.fast, s);
+	if(v.q==27) return v.trt ? sc_ext_x<ST, 27, true, XB>(v.ext, a, kind, v.fast, s) : sc_ext_x<ST, 27, false, XB>(v.ext, a, kind, v.fast, s);
 	return cudaErrorInvalidValue;
 }
 
@@ -643,36 +715,44 @@ template<int ST> cudaError_t launch_stream_collide_t(const Variant& v, const Ste
 	int kind = path;
 	if(path==PATH_AUTO) kind = pairs_ok && ST!=ST_FP32 ? PATH_PIPE : PATH_CELLS;
 	if((kind==PATH_ROWS && !rows_ok) || ((kind==PATH_PAIRS||kind==PATH_PIPE) && !pairs_ok)) return cudaErrorInvalidConfiguration;
-	if(v.ext&EXT_SG) return launch_stream_collide_sg<ST>(v, a, kind, s);
+	switch(v.ext&(EXT_SG|EXT_MB)) {
+		case EXT_SG: return launch_stream_collide_x<ST, EXT_SG>(v, a, kind, s);
+		case EXT_MB: return launch_stream_collide_x<ST, EXT_MB>(v, a, kind, s);
+		case EXT_SG|EXT_MB: return launch_stream_collide_x<ST, EXT_SG|EXT_MB>(v, a, kind, s);
+		default: break;
+	}
 	if(v.q==19) return v.trt ? sc_ext<ST, 19, true>(v.ext, a, kind, v.fast, s) : sc_ext<ST, 19, false>(v.ext, a, kind, v.fast, s);
 	if(v.q==27) return v.trt ? sc_ext<ST, 27, true>(v.ext, a, kind, v.fast, s) : sc_ext<ST, 27, false>(v.ext, a, kind, v.fast, s);
 	return cudaErrorInvalidValue;
 }
 
-template<int ST, int Q, int EXT> inline void uf_launch(const StepArgs& a, const bool fast, cudaStream_t s) {
-	if(fast) k_update_fields<Q, ST, EXT, true><<<cell_grid(a.g), BLOCK, 0, s>>>(a);
-	else k_update_fields<Q, ST, EXT, false><<<cell_grid(a.g), BLOCK, 0, s>>>(a);
+template<int ST, int Q, int EXT> inline void uf_launch(const StepArgs& a, const bool fast, const bool mb, cudaStream_t s) {
+	if(fast) k_update_fields<Q, ST, EXT, true><<<cell_grid(a.g), BLOCK, 0, s>>>(a, mb);
+	else k_update_fields<Q, ST, EXT, false><<<cell_grid(a.g), BLOCK, 0, s>>>(a, mb);
 }
-template<int ST, int Q> inline bool uf_ext(const int ext, const StepArgs& a, const bool fast, cudaStream_t s) {
+template<int ST, int Q> inline bool uf_ext(const int ext, const StepArgs& a, const bool fast, const bool mb, cudaStream_t s) {
 	switch(ext) {
-		case 0:                        uf_launch<ST, Q, 0>(a, fast, s); return true;
-		case EXT_VF:                   uf_launch<ST, Q, EXT_VF>(a, fast, s); return true;
-		case EXT_VF|EXT_FF:            uf_launch<ST, Q, EXT_VF|EXT_FF>(a, fast, s); return true;
-		case EXT_EQ:                   uf_launch<ST, Q, EXT_EQ>(a, fast, s); return true;
-		case EXT_EQ|EXT_VF:            uf_launch<ST, Q, EXT_EQ|EXT_VF>(a, fast, s); return true;
-		case EXT_EQ|EXT_VF|EXT_FF:     uf_launch<ST, Q, EXT_EQ|EXT_VF|EXT_FF>(a, fast, s); return true;
+		case 0:                        uf_launch<ST, Q, 0>(a, fast, mb, s); return true;
+		case EXT_VF:                   uf_launch<ST, Q, EXT_VF>(a, fast, mb, s); return true;
+		case EXT_VF|EXT_FF:            uf_launch<ST, Q, EXT_VF|EXT_FF>(a, fast, mb, s); return true;
+		case EXT_EQ:                   uf_launch<ST, Q, EXT_EQ>(a, fast, mb, s); return true;
+		case EXT_EQ|EXT_VF:            uf_launch<ST, Q, EXT_EQ|EXT_VF>(a, fast, mb, s); return true;
+		case EXT_EQ|EXT_VF|EXT_FF:     uf_launch<ST, Q, EXT_EQ|EXT_VF|EXT_FF>(a, fast, mb, s); return true;
 		default: return false;
 	}
 }
 template<int ST> cudaError_t launch_update_fields_t(const Variant& v, const StepArgs& a, cudaStream_t s) {
-	const int ext = v.ext&~EXT_SG; // SUBGRID changes only the collision
-	const bool ok = v.q==19 ? uf_ext<ST, 19>(ext, a, v.fast, s) : v.q==27 ? uf_ext<ST, 27>(ext, a, v.fast, s) : false;
+	const int ext = v.ext&~(EXT_SG|EXT_MB); // SUBGRID changes only the collision; MOVING_BOUNDARIES is a run-time switch here
+	const bool mb = (v.ext&EXT_MB)!=0;
+	const bool ok = v.q==19 ? uf_ext<ST, 19>(ext, a, v.fast, mb, s) : v.q==27 ? uf_ext<ST, 27>(ext, a, v.fast, mb, s) : false;
 	return ok ? cudaGetLastError() : cudaErrorInvalidValue;
 }
 
 template<int ST> cudaError_t launch_initialize_t(const Variant& v, const StepArgs& a, cudaStream_t s) {
-	if(v.q==19) k_initialize<19, ST><<<cell_grid(a.g), BLOCK, 0, s>>>(a);
-	else if(v.q==27) k_initialize<27, ST><<<cell_grid(a.g), BLOCK, 0, s>>>(a);
+	uint8_t* flags = const_cast<uint8_t*>(a.flags); // the domain's own flags array: initialize marks TYPE_MS cells
+	const bool mb = (v.ext&EXT_MB)!=0;
+	if(v.q==19) k_initialize<19, ST><<<cell_grid(a.g), BLOCK, 0, s>>>(a, flags, mb);
+	else if(v.q==27) k_initialize<27, ST><<<cell_grid(a.g), BLOCK, 0, s>>>(a, flags, mb);
 	else return cudaErrorInvalidValue;
 	return cudaGetLastError();
 }
@@ -685,9 +765,9 @@ template<int ST> cudaError_t launch_update_force_field_t(const Variant& v, const
 
 } // namespace fx3d
 
-#define FX3D_DEFINE_SG_LAUNCHER(ST) \
+#define FX3D_DEFINE_X_LAUNCHER(ST, XB) \
 	namespace fx3d { \
-	template<> cudaError_t launch_stream_collide_sg<ST>(const Variant& v, const StepArgs& a, const int kind, cudaStream_t s) { return launch_stream_collide_sg_t<ST>(v, a, kind, s); } \
+	template<> cudaError_t launch_stream_collide_x<ST, XB>(const Variant& v, const StepArgs& a, const int kind, cudaStream_t s) { return launch_stream_collide_x_t<ST, XB>(v, a, kind, s); } \
 	}
 
 #define FX3D_DEFINE_LAUNCHERS(sfx, ST) \

@@ -1,4 +1,4 @@
-// SUBGRID (Smagorinsky-Lilly) variants of stream_collide for FP16S storage, compiled apart from
-// lbm_kernels_fp16s.cu so that the two halves build in parallel.
+// SUBGRID variants of stream_collide, FP16S DDF storage
 #include "lbm_kernels.cuh"
-FX3D_DEFINE_SG_LAUNCHER(fx3d::ST_FP16S)
+
+FX3D_DEFINE_X_LAUNCHER(fx3d::ST_FP16S, fx3d::EXT_SG)

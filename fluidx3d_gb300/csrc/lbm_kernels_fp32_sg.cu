@@ -1,4 +1,4 @@
-// SUBGRID (Smagorinsky-Lilly) variants of stream_collide for FP32 storage, compiled apart from
-// lbm_kernels_fp32.cu so that the two halves build in parallel.
+// SUBGRID variants of stream_collide, FP32 DDF storage
 #include "lbm_kernels.cuh"
-FX3D_DEFINE_SG_LAUNCHER(fx3d::ST_FP32)
+
+FX3D_DEFINE_X_LAUNCHER(fx3d::ST_FP32, fx3d::EXT_SG)

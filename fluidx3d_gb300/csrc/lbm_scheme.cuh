@@ -50,6 +50,12 @@ template<int I> __device__ __forceinline__ float csum(const float vx, const floa
 	return s;
 }
 
+// c_I.v as the reference writes it in apply_moving_boundaries: c(I)*vx+c(N+I)*vy+c(2N+I)*vz with the
+// velocities as FP32 constants, each product rounded (exact), summed left to right
+template<int I> __device__ __forceinline__ float cdot(const float vx, const float vy, const float vz) {
+	return __fadd_rn(__fadd_rn(__fmul_rn((float)vs_c(0, I), vx), __fmul_rn((float)vs_c(1, I), vy)), __fmul_rn((float)vs_c(2, I), vz));
+}
+
 // ---------------------------------------------------------------- DDF storage codecs
 template<int ST> struct Codec;
 template<> struct Codec<ST_FP32> {

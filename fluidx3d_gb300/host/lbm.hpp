@@ -4,7 +4,8 @@
 //
 // The variant is chosen the way the reference chooses it, with macros defined before this header
 // is included (src/defines.hpp:5-29): D3Q19 (default) or D3Q27; SRT (default) or TRT; FP16S or
-// FP16C DDF storage (default FP32); VOLUME_FORCE, FORCE_FIELD, EQUILIBRIUM_BOUNDARIES, SUBGRID; and, new here,
+// FP16C DDF storage (default FP32); VOLUME_FORCE, FORCE_FIELD, EQUILIBRIUM_BOUNDARIES, SUBGRID, MOVING_BOUNDARIES;
+// and, new here,
 // EXACT_ARITHMETIC / FAST_ARITHMETIC (default: exact with FP32 storage, fast with FP16S/FP16C).
 //
 // Errors: the reference prints and exits (src/utilities.hpp:4159-4166); here a failed call throws
@@ -135,6 +136,9 @@ inline lbm_config lbm_config_from_defines(const uint Nx, const uint Ny, const ui
 #if defined(EQUILIBRIUM_BOUNDARIES)
 	c.extensions |= LBM_EXT_EQUILIBRIUM_BOUNDARIES;
 #endif
+#if defined(MOVING_BOUNDARIES)
+	c.extensions |= LBM_EXT_MOVING_BOUNDARIES;
+#endif
 #if defined(SUBGRID)
 	c.extensions |= LBM_EXT_SUBGRID;
 #endif
@@ -237,6 +241,12 @@ public:
 
 	void update_force_field() { lbm_check(lbm_update_force_field(domain)); lbm_check(lbm_synchronize(domain)); }
 	void reset_force_field() { lbm_check(lbm_reset_force_field(domain)); }
+#if defined(MOVING_BOUNDARIES)
+	void update_moving_boundaries() { // src/lbm.cpp:1019-1023
+		lbm_check(lbm_update_moving_boundaries(domain));
+		if(!initialized) flags.read_from_device();
+	}
+#endif
 	float3 object_center_of_mass(const uchar flag_marker=TYPE_S) {
 		double o[4];
 		lbm_check(lbm_object_center_of_mass(domain, flag_marker, o));

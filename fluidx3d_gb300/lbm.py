@@ -164,6 +164,15 @@ class LBM:
     def reset_force_field(self):
         self._check(C.load().lbm_reset_force_field(self._d))
 
+    # ------------------------------------------------------------------ moving boundaries (src/lbm.cpp:1019-1023)
+    def update_moving_boundaries(self):
+        """Marks the cells next to TYPE_S cells with u != 0 as TYPE_MS (and unmarks the others) after
+        the solids' velocities changed; needs the "moving_boundaries" extension. Host copies of the
+        flags follow before initialization, as after voxelization."""
+        self._check(C.load().lbm_update_moving_boundaries(self._d))
+        if not self.initialized:
+            self.flags.read_from_device()
+
     def object_center_of_mass(self, flag_marker=TYPE_S):
         out = (ctypes.c_double * 4)()
         self._check(C.load().lbm_object_center_of_mass(self._d, flag_marker, out))

@@ -8,7 +8,9 @@ setups (src/setup.cpp) where one exists:
   * ``sphere_channel``: x-channel with TYPE_E inlet/outlet planes, TYPE_S y/z walls and a TYPE_S
     sphere (src/shapes.cpp:5-8 ``sphere``) marked TYPE_S|TYPE_X for force summation
     (src/setup.cpp:148-187 pattern);
-  * ``empty_box``: the reference benchmark's periodic empty box (src/setup.cpp:5-36).
+  * ``empty_box``: the reference benchmark's periodic empty box (src/setup.cpp:5-36);
+  * ``lid_driven_cavity`` and ``taylor_couette``: the reference's MOVING_BOUNDARIES setups
+    (src/setup.cpp:236-247 and 212-229), solid walls with a velocity.
 """
 from __future__ import annotations
 
@@ -86,3 +88,51 @@ def box_filter_noise(Nx, Ny, Nz, sigma, width=5, seed=0):
             a = acc / width
         out.append(a.reshape(-1))
     return np.concatenate(out).astype(np.float32)
+
+
+def lid_driven_cavity(Nx, Ny, Nz, u_lid=0.1):
+    """src/setup.cpp:236-247: TYPE_S on all six faces, u_y = u_lid on the plane z = Nz-1 (the moving
+    lid; with MOVING_BOUNDARIES the cells below it become TYPE_MS)."""
+    N = Nx * Ny * Nz
+    x, y, z = coords(Nx, Ny, Nz)
+    flags = np.zeros(N, np.uint8)
+    flags[(x == 0) | (x == Nx - 1) | (y == 0) | (y == Ny - 1) | (z == 0) | (z == Nz - 1)] = TYPE_S
+    u = np.zeros(3 * N, np.float32)
+    u[N:2 * N][z == Nz - 1] = np.float32(u_lid)
+    return dict(rho=np.ones(N, np.float32), u=u, flags=flags, F=np.zeros(3 * N, np.float32))
+
+
+def _z_cylinder(Nx, Ny, Nz, radius):
+    """src/shapes.cpp:21-26 cylinder() about the box centre with axis (0,0,Nz), in FP32 and the
+    reference's operation order: (tx^2+ty^2+tz^2) - tz^2 <= r^2."""
+    x, y, z = coords(Nx, Ny, Nz)
+    f = np.float32
+    tx = x.astype(f) - f(0.5 * Nx - 0.5)
+    ty = y.astype(f) - f(0.5 * Ny - 0.5)
+    tz = z.astype(f) - f(0.5 * Nz - 0.5)
+    sqnt = tz * tz
+    dist = ((tx * tx + ty * ty) + tz * tz) - sqnt
+    r = f(radius)
+    return (dist <= r * r) & (sqnt <= f(0.5 * Nz) * f(0.5 * Nz))
+
+
+def taylor_couette(Nx, Ny, Nz, seed=42):
+    """src/setup.cpp:212-229: TYPE_S outside the cylinder of radius Nx/2-1 (at rest) and inside the
+    cylinder of radius Nx/4, which rotates: u = (p_y, -p_x, small noise) with p the box-relative
+    position in [-0.5, 0.5]^3 (src/lbm.hpp:528-530). The noise on u_z (+-0.001) is seeded numpy noise in
+    place of the reference's own generator."""
+    N = Nx * Ny * Nz
+    x, y, z = coords(Nx, Ny, Nz)
+    flags = np.zeros(N, np.uint8)
+    flags[~_z_cylinder(Nx, Ny, Nz, Nx // 2 - 1)] = TYPE_S
+    inner = _z_cylinder(Nx, Ny, Nz, Nx // 4)
+    f = np.float32
+    px = (x.astype(f) + f(0.5)) / f(Nx) - f(0.5)
+    py = (y.astype(f) + f(0.5)) / f(Ny) - f(0.5)
+    rng = np.random.default_rng(seed)
+    u = np.zeros(3 * N, np.float32)
+    u[:N][inner] = py[inner]
+    u[N:2 * N][inner] = -px[inner]
+    u[2 * N:][inner] = ((1.0 - rng.uniform(0.0, 2.0, N)) * 0.001).astype(np.float32)[inner]
+    flags[inner] = TYPE_S
+    return dict(rho=np.ones(N, np.float32), u=u, flags=flags, F=np.zeros(3 * N, np.float32))

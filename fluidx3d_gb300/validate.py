@@ -6,6 +6,7 @@ the reference's validation setups, src/setup.cpp:40-187), printing one JSON obje
     python -m fluidx3d_gb300.validate large        # 2048x1024x1280 FP16C with a voxelized 200k-triangle mesh
     python -m fluidx3d_gb300.validate adjoint      # 128x64x64 channel, dJ/dF of the outlet-plane kinetic energy
     python -m fluidx3d_gb300.validate adjoint_scale  # sphere channel, dJ/dF of the sphere drag, FP16S
+    python -m fluidx3d_gb300.validate variants     # sphere channel: time per step of the extension variants
 
 All inputs are synthetic and seeded. Timings use CUDA events on the solver's stream.
 """
@@ -177,9 +178,53 @@ def adjoint_scale(steps=10000, window=None, interval=200, storage="fp16s"):
                 gradient_over_forward=total / t.ms), grad
 
 
+VARIANTS = [("fp16s", ("eq",)), ("fp16s", ("eq", "mb")), ("fp16s", ("eq", "sg")), ("fp16s", ("eq", "mb", "sg")),
+            ("fp16c", ("eq", "mb")), ("fp32", ("eq",)), ("fp32", ("eq", "mb"))]
+
+
+def variants(steps=200, warmup=20, sphere_uy=0.02):
+    """The C2 sphere channel (512x256x256, D3Q19 TRT, automatic arithmetic and kernel) with the
+    SUBGRID / MOVING_BOUNDARIES variants; with MOVING_BOUNDARIES the sphere moves at u_y = sphere_uy.
+    Per variant: ms per step over `steps` steps after `warmup`, MLUPs/s, the TYPE_MS cell count and
+    the fraction of the measured HBM peak under the reference's byte accounting."""
+    import os
+    peak = None
+    try:
+        root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+        with open(os.path.join(root, "MEASURED_PEAKS.json")) as fh:
+            peak = float(json.load(fh)["hbm_gbs"])
+    except (OSError, KeyError, ValueError):
+        pass
+    Nx, Ny, Nz = 512, 256, 256
+    N = Nx * Ny * Nz
+    f = S.sphere_channel(Nx, Ny, Nz, u_in=0.075, radius=32.0, center=(128.0, 128.0, 128.0))
+    moving_u = f["u"].copy()
+    moving_u[N:2 * N][(f["flags"] & TYPE_X) != 0] = np.float32(sphere_uy)
+    out = []
+    for storage, ext in VARIANTS:
+        with LBM(Nx, Ny, Nz, 0.048, collision="trt", storage=storage, extensions=ext) as lbm:
+            lbm.rho.data[:], lbm.flags.data[:] = f["rho"], f["flags"]
+            lbm.u.data[:] = moving_u if "mb" in ext else f["u"]
+            lbm.run(warmup)
+            with Timer(lbm) as t:
+                lbm.run(steps)
+            ms = t.ms / steps
+            marked = 0
+            if "mb" in ext:
+                lbm.flags.read_from_device()
+                marked = int(np.count_nonzero((lbm.flags.data & 3) == 3))
+            bpc = lbm.bandwidth_bytes_per_cell()
+            r = dict(storage=storage, extensions=list(ext), ms_per_step=ms, mlups=N / (ms * 1e-3) / 1e6, ms_cells=marked,
+                     bytes_per_cell=bpc)
+            if peak:
+                r["hbm_fraction"] = bpc * N / (ms * 1e-3) / 1e9 / peak
+            out.append(r)
+    return dict(run="variants", cells=N, steps=steps, results=out)
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("run", choices=["tgv", "sphere", "large", "adjoint", "adjoint_scale"])
+    ap.add_argument("run", choices=["tgv", "sphere", "large", "adjoint", "adjoint_scale", "variants"])
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--storage", default=None)
     args = ap.parse_args(argv)
@@ -197,6 +242,8 @@ def main(argv=None):
         lbm.close()
     elif args.run == "adjoint":
         out = adjoint(**{k: v for k, v in kw.items() if k != "storage"})[0]
+    elif args.run == "variants":
+        out = variants(**{k: v for k, v in kw.items() if k != "storage"})
     else:
         out = adjoint_scale(**kw)[0]
     print(json.dumps(out))

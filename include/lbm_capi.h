@@ -36,7 +36,8 @@ typedef enum lbm_status {
 	LBM_ERR_CUDA = 3,             /* a CUDA runtime call failed */
 	LBM_ERR_NOT_INITIALIZED = 4,  /* the call needs lbm_initialize first */
 	LBM_ERR_UNSUPPORTED = 5,      /* the variant lacks the extension the call needs */
-	LBM_ERR_NO_DEVICE = 6         /* no CUDA device (the reference exits in get_devices, src/opencl.hpp:222-252) */
+	LBM_ERR_NO_DEVICE = 6,        /* no CUDA device (the reference exits in get_devices, src/opencl.hpp:222-252) */
+	LBM_ERR_IO = 7                /* a file could not be opened or written */
 } lbm_status;
 
 /* variant selection: the reference's compile-time switches (src/defines.hpp:5-29) as runtime values */
@@ -46,7 +47,9 @@ enum {
 	LBM_EXT_VOLUME_FORCE = 1,          /* VOLUME_FORCE: global force (fx,fy,fz), Guo forcing */
 	LBM_EXT_FORCE_FIELD = 2,           /* FORCE_FIELD: per-cell force F added to (fx,fy,fz) */
 	LBM_EXT_EQUILIBRIUM_BOUNDARIES = 4, /* EQUILIBRIUM_BOUNDARIES: TYPE_E cells held at their rho/u */
-	LBM_EXT_SUBGRID = 8                /* SUBGRID: Smagorinsky-Lilly relaxation rate per cell (src/kernel.cpp:1579-1593); not with lbm_run_adjoint */
+	LBM_EXT_SUBGRID = 8,               /* SUBGRID: Smagorinsky-Lilly relaxation rate per cell (src/kernel.cpp:1579-1593); not with lbm_run_adjoint */
+	LBM_EXT_MOVING_BOUNDARIES = 16     /* MOVING_BOUNDARIES: TYPE_S cells with u != 0 are moving walls for their TYPE_MS
+	                                    * neighbours (src/kernel.cpp:1104-1113, 1378-1387, 1431-1450); not with lbm_run_adjoint */
 };
 /* arithmetic of the collision. EXACT evaluates the reference's FP32 operation order with IEEE
  * rounding at every step: bit-identical to the reference's kernel text evaluated on a CPU. FAST
@@ -108,6 +111,22 @@ int lbm_set_force(lbm_domain* domain, float fx, float fy, float fz); /* LBM::set
 int lbm_is_initialized(lbm_domain* domain, int* initialized);
 int lbm_reset(lbm_domain* domain); /* next lbm_initialize starts over (src/lbm.cpp:982-984) */
 
+/* ---- VTK export (src/lbm.hpp:298-340 Memory_Container::write_vtk, 401-407 write_device_to_vtk):
+ * writes field rho, u, flags or F as a binary legacy VTK file (STRUCTURED_POINTS, big-endian, one
+ * point per cell, x fastest; u and F interleaved per point) with the reference's header: title
+ * "FluidX3D <file name>", origin spacing*(0.5-N/2) per axis, `spacing` between points. FP32 values
+ * are multiplied by `scale` (the reference's SI unit conversion; 1 for lattice units) on the GPU,
+ * where they are also byte-swapped and interleaved, chunk by chunk, while the previous chunk is
+ * written to the file. rho/u are brought up to date first (update_fields). The file's folder is
+ * created if missing; the caller builds the file name (the reference: <path><name>-<t, 9 digits>.vtk). */
+int lbm_write_vtk(lbm_domain* domain, int field, const char* filename, float spacing, float scale);
+
+/* ---- moving boundaries (LBM_EXT_MOVING_BOUNDARIES; src/lbm.cpp:240-244, 1019-1023; src/kernel.cpp:1431-1450):
+ * sets TYPE_MS on every cell (not TYPE_S, TYPE_E or TYPE_T) that has a TYPE_S neighbour with u != 0
+ * and clears it on the others; call it after changing the velocity of solid cells. lbm_initialize
+ * does the same marking (TYPE_T cells included, as the reference's initialize does). */
+int lbm_update_moving_boundaries(lbm_domain* domain);
+
 /* ---- forces on solids (src/lbm.cpp:207-229, 991-1015; src/kernel.cpp:1873-1959) */
 /* F = momentum exchange on TYPE_S cells at the current t (skipped if already current) */
 int lbm_update_force_field(lbm_domain* domain);
@@ -139,6 +158,8 @@ int lbm_object_sum_static(int device, uint32_t Nx, uint32_t Ny, uint32_t Nz, con
  * Cells inside get flags = (flags & ~(TYPE_S|TYPE_E)) | flag. */
 int lbm_voxelize_mesh(lbm_domain* domain, const float* p0, const float* p1, const float* p2, uint32_t triangles, uint8_t flag,
                       const float center[3], const float linear_velocity[3], const float rotational_velocity[3]);
+/* With LBM_EXT_MOVING_BOUNDARIES, a solid (flag & (TYPE_S|TYPE_E) == TYPE_S) voxelized with a non-zero
+ * velocity also runs lbm_update_moving_boundaries (src/lbm.cpp:1082-1084). */
 /* clears `flag` in the mesh bounding box +-1 cell */
 int lbm_unvoxelize_mesh(lbm_domain* domain, const float pmin[3], const float pmax[3], uint8_t flag);
 

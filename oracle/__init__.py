@@ -24,7 +24,7 @@ LIB = os.path.join(BUILD, "liblbm_oracle.so")
 REF_DIR = os.path.join(HERE, "_ref")
 
 STORAGE = {"fp32": 0, "fp16s": 1, "fp16c": 2}
-EXT_BITS = {"vf": 1, "ff": 2, "eq": 4, "sg": 8}
+EXT_BITS = {"vf": 1, "ff": 2, "eq": 4, "sg": 8, "mb": 16}
 
 
 def build_oracle(force: bool = False) -> str:
@@ -66,6 +66,7 @@ def lib() -> ctypes.CDLL:
             getattr(L, f"oracle_run_{s}").argtypes = [cfg, v, v, v, v, u64, u64, r, r, r, v]
             getattr(L, f"oracle_update_fields_{s}").argtypes = [cfg, v, v, v, v, u64, r, r, r, v]
             getattr(L, f"oracle_update_force_field_{s}").argtypes = [cfg, v, v, u64, v]
+            getattr(L, f"oracle_update_moving_boundaries_{s}").argtypes = [cfg, v, v]
         L.oracle_object_sum.argtypes = [cfg, ctypes.c_int, v, v, u8, d, d, d, v]
         L.oracle_voxelize_mesh.argtypes = [cfg, u32, v, v, v, u64, u8, v, v, v, v]
         L.oracle_voxelize_rays.argtypes = [cfg, u32, v, v, v, u64, u8, v, v, v, v, v, u64]
@@ -138,6 +139,9 @@ class Oracle:
         self._chk(self._fn("update_force_field")(ctypes.byref(self.cfg), _p(self.fi), _p(self.flags), self.t, _p(self.F)),
                   "update_force_field")
 
+    def update_moving_boundaries(self):
+        self._chk(self._fn("update_moving_boundaries")(ctypes.byref(self.cfg), _p(self.u), _p(self.flags)), "update_moving_boundaries")
+
     def object_sum(self, kind, marker, center=(0.0, 0.0, 0.0)):
         out = np.zeros(4, dtype=np.float64)
         F = np.ascontiguousarray(self.F, dtype=np.float32)
@@ -193,6 +197,7 @@ class RefHarness:
         L.ref_stream_collide.argtypes = [v, v, v, v, u64, f32, f32, f32, v]
         L.ref_update_fields.argtypes = [v, v, v, v, u64, f32, f32, f32, v]
         L.ref_update_force_field.argtypes = [v, v, u64, v]
+        L.ref_update_moving_boundaries.argtypes = [v, v]
         L.ref_voxelize_mesh.argtypes = [u32, v, v, v, u64, u8, v, v, v, v]
         L.ref_unvoxelize_mesh.argtypes = [v, u8, f32, f32, f32, f32, f32, f32]
         self.L = L
@@ -229,6 +234,11 @@ class RefHarness:
         self._cfg()
         if self.L.ref_update_force_field(_p(self.fi), _p(self.flags), self.t, _p(self.F)) != 0:
             raise RuntimeError("update_force_field needs the FORCE_FIELD variant")
+
+    def update_moving_boundaries(self):
+        self._cfg()
+        if self.L.ref_update_moving_boundaries(_p(self.u), _p(self.flags)) != 0:
+            raise RuntimeError("update_moving_boundaries needs the MOVING_BOUNDARIES variant")
 
     def voxelize_mesh(self, direction, flag, p0, p1, p2, bbu, t):
         self._cfg()

@@ -10,7 +10,9 @@
 //   calculate_forcing_terms          src/kernel.cpp:1091-1101
 //   load_f / store_f (Esoteric-Pull) src/kernel.cpp:1326-1339
 //   initialize                       src/kernel.cpp:1358-1430
-//   stream_collide (SRT/TRT, TYPE_S, TYPE_E, VOLUME_FORCE, FORCE_FIELD)  src/kernel.cpp:1454-1636
+//   stream_collide (SRT/TRT, TYPE_S, TYPE_E, VOLUME_FORCE, FORCE_FIELD, SUBGRID)  src/kernel.cpp:1454-1636
+//   apply_moving_boundaries          src/kernel.cpp:1104-1113
+//   update_moving_boundaries         src/kernel.cpp:1431-1450
 //   update_fields                    src/kernel.cpp:1794-1870
 //   update_force_field               src/kernel.cpp:1873-1884
 //   object_center_of_mass/force/torque (sums done in FP64 here)  src/kernel.cpp:1901-1959
@@ -40,8 +42,8 @@ typedef uint32_t u32;
 typedef uint64_t u64;
 
 enum { ST_FP32 = 0, ST_FP16S = 1, ST_FP16C = 2 };
-enum { EXT_VOLUME_FORCE = 1, EXT_FORCE_FIELD = 2, EXT_EQUILIBRIUM_BOUNDARIES = 4, EXT_SUBGRID = 8 };
-enum { T_S = 0x01, T_E = 0x02, T_BO = 0x03, T_MS = 0x03, T_G = 0x20, T_SU = 0x38, T_XY = 0xC0 };
+enum { EXT_VOLUME_FORCE = 1, EXT_FORCE_FIELD = 2, EXT_EQUILIBRIUM_BOUNDARIES = 4, EXT_SUBGRID = 8, EXT_MOVING_BOUNDARIES = 16 };
+enum { T_S = 0x01, T_E = 0x02, T_T = 0x04, T_BO = 0x03, T_MS = 0x03, T_G = 0x20, T_SU = 0x38, T_XY = 0xC0 };
 
 extern "C" struct OracleConfig {
 	u32 Nx, Ny, Nz;
@@ -237,16 +239,65 @@ template<typename real> static void forcing_terms(const real ux, const real uy, 
 }
 
 // ------------------------------------------------------------------ kernels
+// TYPE_MS marking (src/kernel.cpp:1381-1385, 1441-1447): a cell next to a TYPE_S cell with u != 0
+template<typename real> static bool next_to_moving_boundary(const u64* j, const real* u, const u8* flags, const u32 q, const u64 N) {
+	bool next = false;
+	for(u32 i=1u; i<q; i++) next = next||((flags[j[i]]&T_BO)==T_S&&(u[j[i]]!=(real)0||u[N+j[i]]!=(real)0||u[2ull*N+j[i]]!=(real)0));
+	return next;
+}
+
 template<typename real> static int initialize_t(const OracleConfig* c, void* fi, real* rho, real* u, u8* flags) {
 	const Grid G(c); const u32 q = c->q;
+	const bool mb = (c->ext&EXT_MOVING_BOUNDARIES)!=0u;
+	// MOVING_BOUNDARIES rewrites flags while neighbours read them; the TYPE_S bit pattern a neighbour
+	// tests never changes (00 <-> 11), so marking into a copy gives the reference's result race-free
+	std::vector<u8> marked(mb ? G.N : 0ull);
 	parallel_cells(G.N, c->threads, [&](const u64 n) {
 		u64 j[27]; G.neighbors(n, q, j);
-		if((flags[n]&T_BO)==T_S) { u[n] = (real)0; u[G.N+n] = (real)0; u[2ull*G.N+n] = (real)0; } // src/kernel.cpp:1370-1373
+		const u8 flagsn_bo = flags[n]&T_BO;
+		if(mb) {
+			marked[n] = flags[n];
+			if(flagsn_bo==T_S) { // solid cells keep their (wall) velocity unless all their neighbours are solid (src/kernel.cpp:1370-1374)
+				bool only_s = true;
+				for(u32 i=1u; i<q; i++) only_s = only_s&&(flags[j[i]]&T_BO)==T_S;
+				if(only_s) { u[n] = (real)0; u[G.N+n] = (real)0; u[2ull*G.N+n] = (real)0; }
+			} else if(flagsn_bo!=T_E) {
+				marked[n] = next_to_moving_boundary<real>(j, u, flags, q, G.N) ? (u8)(flags[n]|T_MS) : (u8)(flags[n]&~T_MS);
+			}
+		} else if(flagsn_bo==T_S) { u[n] = (real)0; u[G.N+n] = (real)0; u[2ull*G.N+n] = (real)0; } // src/kernel.cpp:1370-1377
 		real feq[27];
 		calculate_f_eq<real>(rho[n], u[n], u[G.N+n], u[2ull*G.N+n], feq, q);
 		store_f<real>(n, feq, fi, j, 1ull, q, G.N, c->storage); // odd parity baked in (src/kernel.cpp:1429)
 	});
+	if(mb) std::memcpy(flags, marked.data(), G.N);
 	return 0;
+}
+
+// src/kernel.cpp:1431-1450: fluid cells (not TYPE_S, TYPE_E or TYPE_T) next to a moving solid get TYPE_MS
+template<typename real> static int update_moving_boundaries_t(const OracleConfig* c, const real* u, u8* flags) {
+	const Grid G(c); const u32 q = c->q;
+	std::vector<u8> marked(flags, flags+G.N);
+	parallel_cells(G.N, c->threads, [&](const u64 n) {
+		const u8 flagsn = flags[n], flagsn_bo = flagsn&T_BO;
+		if(flagsn_bo==T_S||flagsn_bo==T_E||(flagsn&T_T)) return;
+		u64 j[27]; G.neighbors(n, q, j);
+		marked[n] = next_to_moving_boundary<real>(j, u, flags, q, G.N) ? (u8)(flagsn|T_MS) : (u8)(flagsn&~T_MS);
+	});
+	std::memcpy(flags, marked.data(), G.N);
+	return 0;
+}
+
+// src/kernel.cpp:1104-1113 apply_moving_boundaries: in a TYPE_MS cell, population i gains
+// -6 w_i (c_{i+1}.u_s) when the neighbour along c_{i+1} is a TYPE_S cell moving at u_s, population
+// i+1 gains -6 w_i (c_i.u_s) from the neighbour along c_i (i odd, wall density 1)
+template<typename real> static void apply_moving_boundaries(real* fhn, const u64* j, const real* u, const u8* flags, const u32 q, const u64 N) {
+	const Weights<real> W = weights<real>(q);
+	auto cu = [&](const u32 k, const u64 s) { return (real)cq(q, 0, k)*u[s]+(real)cq(q, 1, k)*u[N+s]+(real)cq(q, 2, k)*u[2ull*N+s]; };
+	for(u32 i=1u; i<q; i+=2u) {
+		const real w6 = (real)(-6)*weight(W, i);
+		if((flags[j[i+1u]]&T_BO)==T_S) fhn[i] = fmaT(w6, cu(i+1u, j[i+1u]), fhn[i]);
+		if((flags[j[i]]&T_BO)==T_S) fhn[i+1u] = fmaT(w6, cu(i, j[i]), fhn[i+1u]);
+	}
 }
 
 // force shift + clamp shared by stream_collide and update_fields (src/kernel.cpp:1550-1563, 1852-1862)
@@ -307,12 +358,14 @@ template<typename real> static int stream_collide_t(const OracleConfig* c, void*
                                                     const real fx, const real fy, const real fz, const real* F) {
 	const Grid G(c); const u32 q = c->q;
 	const bool eq = (c->ext&EXT_EQUILIBRIUM_BOUNDARIES)!=0u, ff = (c->ext&EXT_FORCE_FIELD)!=0u, vf = (c->ext&EXT_VOLUME_FORCE)!=0u;
+	const bool mb = (c->ext&EXT_MOVING_BOUNDARIES)!=0u;
 	parallel_cells(G.N, c->threads, [&](const u64 n) {
 		const u8 flagsn_bo = flags[n]&T_BO;
 		if(flagsn_bo==T_S||(flags[n]&T_SU)==T_G) return; // solid (implicit bounce-back through Esoteric-Pull) or gas: nothing
 		u64 j[27]; G.neighbors(n, q, j);
 		real fhn[27];
 		load_f<real>(n, fhn, fi, j, t, q, G.N, c->storage);
+		if(mb && flagsn_bo==T_MS) apply_moving_boundaries<real>(fhn, j, u, flags, q, G.N);
 		real rhon, uxn, uyn, uzn;
 		const bool is_e = eq && flagsn_bo==T_E;
 		if(is_e) { rhon = rho[n]; uxn = u[n]; uyn = u[G.N+n]; uzn = u[2ull*G.N+n]; }
@@ -330,12 +383,14 @@ template<typename real> static int update_fields_t(const OracleConfig* c, const 
                                                    const real fx, const real fy, const real fz, const real* F) {
 	const Grid G(c); const u32 q = c->q;
 	const bool eq = (c->ext&EXT_EQUILIBRIUM_BOUNDARIES)!=0u, ff = (c->ext&EXT_FORCE_FIELD)!=0u, vf = (c->ext&EXT_VOLUME_FORCE)!=0u;
+	const bool mb = (c->ext&EXT_MOVING_BOUNDARIES)!=0u;
 	parallel_cells(G.N, c->threads, [&](const u64 n) {
 		const u8 flagsn_bo = flags[n]&T_BO;
 		if(flagsn_bo==T_S||(flags[n]&T_SU)==T_G) return;
 		u64 j[27]; G.neighbors(n, q, j);
 		real fhn[27];
 		load_f<real>(n, fhn, fi, j, t, q, G.N, c->storage);
+		if(mb && flagsn_bo==T_MS) apply_moving_boundaries<real>(fhn, j, u, flags, q, G.N);
 		real rhon, uxn, uyn, uzn;
 		calculate_rho_u<real>(fhn, rhon, uxn, uyn, uzn, q);
 		real fxn = fx, fyn = fy, fzn = fz;
@@ -530,6 +585,8 @@ int oracle_update_fields_f32(const OracleConfig* c, const void* fi, float* rho, 
 int oracle_update_fields_f64(const OracleConfig* c, const double* fi, double* rho, double* u, const u8* flags, const u64 t, const double fx, const double fy, const double fz, const double* F) {
 	return valid(c) ? update_fields_t<double>(c, fi, rho, u, flags, t, fx, fy, fz, F) : -1;
 }
+int oracle_update_moving_boundaries_f32(const OracleConfig* c, const float* u, u8* flags) { return valid(c) ? update_moving_boundaries_t<float>(c, u, flags) : -1; }
+int oracle_update_moving_boundaries_f64(const OracleConfig* c, const double* u, u8* flags) { return valid(c) ? update_moving_boundaries_t<double>(c, u, flags) : -1; }
 int oracle_update_force_field_f32(const OracleConfig* c, const void* fi, const u8* flags, const u64 t, float* F) {
 	return valid(c) ? update_force_field_t<float>(c, fi, flags, t, F) : -1;
 }

@@ -73,7 +73,7 @@ def _defines(q: int, collision: str, storage: str, extensions: tuple[str, ...]) 
     else:
         lines += ["#define fpxx float", "#define fpxx_copy float",
                   "#define load(p,o) (p)[o]", "#define store(p,o,x) (p)[o]=(x)"]
-    ext_macro = {"vf": "VOLUME_FORCE", "ff": "FORCE_FIELD", "eq": "EQUILIBRIUM_BOUNDARIES", "sg": "SUBGRID"}
+    ext_macro = {"vf": "VOLUME_FORCE", "ff": "FORCE_FIELD", "eq": "EQUILIBRIUM_BOUNDARIES", "sg": "SUBGRID", "mb": "MOVING_BOUNDARIES"}
     lines += [f"#define {ext_macro[e]}" for e in extensions]
     return "\n".join(lines) + "\n"
 
@@ -144,6 +144,10 @@ DEFAULT_VARIANTS = [
     (19, "srt", "fp32", ("sg",)),
     (19, "trt", "fp16s", ("eq", "sg")),
     (27, "trt", "fp32", ("eq", "ff", "sg", "vf")),
+    (19, "srt", "fp32", ("mb",)),
+    (19, "trt", "fp16s", ("mb",)),
+    (19, "trt", "fp16c", ("mb", "sg")),
+    (27, "trt", "fp32", ("eq", "ff", "mb", "vf")),
 ]
 
 

@@ -79,6 +79,16 @@ int ref_update_force_field(const void* fi, const u8* flags, const u64 t, float* 
 #endif
 }
 
+int ref_update_moving_boundaries(const float* u, u8* flags) {
+#ifdef MOVING_BOUNDARIES
+	launch(ocl::g_N, [&]() { ocl::update_moving_boundaries(u, flags); });
+	return 0;
+#else
+	(void)u; (void)flags;
+	return -1;
+#endif
+}
+
 void ref_voxelize_mesh(const u32 direction, void* fi, float* u, u8* flags, const u64 t, const u8 flag, const float* p0, const float* p1, const float* p2, const float* bbu) {
 	const u64 A = direction==0u ? (u64)ocl::g_Ny*ocl::g_Nz : direction==1u ? (u64)ocl::g_Nz*ocl::g_Nx : (u64)ocl::g_Nx*ocl::g_Ny;
 	launch(A, [&]() { ocl::voxelize_mesh(direction, (ocl::ddf_t*)fi, u, flags, t, flag, p0, p1, p2, bbu); });

@@ -4,11 +4,13 @@ The generator runs the reference's OpenCL C kernel text compiled for the CPU (or
 built from the reference sources by oracle/ref_harness/build_ref.py) on every case of
 tests/lbm_cases.py and stores what it produced. It needs the reference tree and is run by hand:
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py              # every fixture
+    python tests/golden/make_golden.py CASE [CASE]  # only the lbm_<case>.npz fixtures named
 
 Fixtures:
-  lbm_<case>.npz   rho, u (after update_fields), F (after update_force_field, FORCE_FIELD cases)
-                   and sha256 of the raw DDF bytes, after case.steps time steps
+  lbm_<case>.npz   rho, u (after update_fields), F (after update_force_field, FORCE_FIELD cases),
+                   flags (MOVING_BOUNDARIES cases: TYPE_MS marked by initialize) and sha256 of the raw
+                   DDF bytes, after case.steps time steps
   tgv64.npz        Taylor-Green 64^3 D3Q19 SRT FP32 tau=0.6 after 1000 steps: sha256 of rho/u
                    bytes, u_x at the box centre (the reference's own "binary identity" probe,
                    src/setup.cpp:58), kinetic energy, and a strided sample of u
@@ -49,15 +51,21 @@ def run_case(case, threads=None):
     return h
 
 
-def main():
+def main(names=None):
     build_ref.build_all()
     for case in LC.CASES:
+        if names and case.name not in names:
+            continue
         h = run_case(case)
         out = dict(rho=h.rho, u=h.u, fi_sha256=np.array(sha(h.fi)), steps=np.array(case.steps))
         if "ff" in case.extensions:
             out["F"] = h.F
+        if "mb" in case.extensions:
+            out["flags"] = h.flags
         np.savez_compressed(os.path.join(HERE, f"lbm_{case.name}.npz"), **out)
         print("wrote", case.name)
+    if names:
+        return
     c = LC.TGV64
     h = run_case(c)
     Nx, Ny, Nz = c.shape
@@ -79,4 +87,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

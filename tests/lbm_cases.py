@@ -20,7 +20,7 @@ class Case:
     collision: str
     storage: str
     extensions: tuple = ()
-    geometry: str = "tgv"        # "tgv" | "channel"
+    geometry: str = "tgv"        # "tgv" | "channel" | "cavity" | "couette"
     shape: tuple = (16, 12, 10)
     nu: float = 0.04
     steps: int = 37
@@ -36,8 +36,17 @@ class Case:
         Nx, Ny, Nz = self.shape
         if self.geometry == "tgv":
             c = S.taylor_green(Nx, Ny, Nz)
+        elif self.geometry == "cavity":
+            c = S.lid_driven_cavity(Nx, Ny, Nz, u_lid=0.1)
+        elif self.geometry == "couette":
+            c = S.taylor_couette(Nx, Ny, Nz, seed=self.seed)
         else:
             c = S.sphere_channel(Nx, Ny, Nz, u_in=0.05, radius=3.0, center=(Nx / 3.0, Ny / 2.0, Nz / 2.0))
+            if "sphere_u" in self.extra:  # a moving sphere (MOVING_BOUNDARIES)
+                N = self.N
+                sphere = (c["flags"] & S.TYPE_X) != 0
+                for d, v in enumerate(self.extra["sphere_u"]):
+                    c["u"][d * N:(d + 1) * N][sphere] = np.float32(v)
         if "ff" in self.extensions:
             rng = np.random.default_rng(self.seed)
             c["F"] = rng.normal(0.0, 1e-4, 3 * self.N).astype(np.float32)
@@ -64,6 +73,11 @@ CASES = [
     Case("d3q19_srt_fp32_tgv_sg", 19, "srt", "fp32", ("sg",)),
     Case("d3q19_trt_fp16s_channel_eq_sg", 19, "trt", "fp16s", ("eq", "sg"), "channel"),
     Case("d3q27_trt_fp32_channel_eq_ff_sg_vf", 27, "trt", "fp32", ("eq", "ff", "sg", "vf"), "channel", fx=1e-5),
+    Case("d3q19_srt_fp32_cavity_mb", 19, "srt", "fp32", ("mb",), "cavity"),
+    Case("d3q19_trt_fp16s_couette_mb", 19, "trt", "fp16s", ("mb",), "couette", (16, 16, 12)),
+    Case("d3q19_trt_fp16c_couette_mb_sg", 19, "trt", "fp16c", ("mb", "sg"), "couette", (16, 16, 12), nu=0.01),
+    Case("d3q27_trt_fp32_channel_eq_ff_mb_vf", 27, "trt", "fp32", ("eq", "ff", "mb", "vf"), "channel", fx=1e-5,
+         extra={"sphere_u": (0.0, 0.02, -0.01)}),
 ]
 CASE_BY_NAME = {c.name: c for c in CASES}
 

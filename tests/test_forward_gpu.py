@@ -33,10 +33,10 @@ def make_oracle(case):
 
 
 def skip_unsupported_path(case, path):
-    """SUBGRID runs on the one-cell and the prefetching two-cell kernels only (the row-staged kernel
-    serves the adjoint, which has no SUBGRID)."""
-    if "sg" in case.extensions and path in ("rows", "pairs"):
-        pytest.skip("no SUBGRID variant of this path")
+    """SUBGRID and MOVING_BOUNDARIES run on the one-cell and the prefetching two-cell kernels only
+    (the row-staged kernel serves the adjoint, which has neither)."""
+    if ("sg" in case.extensions or "mb" in case.extensions) and path in ("rows", "pairs"):
+        pytest.skip("no SUBGRID / MOVING_BOUNDARIES variant of this path")
 
 
 @pytest.fixture(params=["rows", "cells"])
@@ -57,6 +57,9 @@ def test_gpu_matches_reference_fixture(case, gpu, golden_dir, path):
         assert np.array_equal(lbm.rho.data, g["rho"])
         assert np.array_equal(lbm.u.data, g["u"])
         assert sha(lbm.read_ddfs()) == str(g["fi_sha256"])
+        if "mb" in case.extensions:
+            lbm.flags.read_from_device()
+            assert np.array_equal(lbm.flags.data, g["flags"])
         if "ff" in case.extensions:
             lbm.update_force_field()
             lbm.F.read_from_device()
@@ -72,6 +75,9 @@ def test_gpu_matches_oracle_step_by_step(case, gpu, path):
         o.initialize()
         lbm.initialize()
         assert np.array_equal(lbm.read_ddfs(), o.fi)
+        if "mb" in case.extensions:  # initialize marks the cells next to moving walls
+            lbm.flags.read_from_device()
+            assert np.array_equal(lbm.flags.data, o.flags) and np.count_nonzero((o.flags & 3) == 3) > 0
         # reading u after initialize runs update_fields first, as the reference's lazy read does
         o.update_fields(*case.force)
         lbm.u.read_from_device()

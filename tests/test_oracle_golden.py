@@ -38,6 +38,9 @@ def test_oracle_matches_reference_fixture(case, golden_dir):
     assert np.array_equal(o.u, g["u"])
     if "ff" in case.extensions:
         assert np.array_equal(o.F, g["F"])
+    if "mb" in case.extensions:
+        assert np.array_equal(o.flags, g["flags"])
+        assert np.count_nonzero((o.flags & 3) == 3) > 0  # cells next to the moving walls are marked
     assert sha(o.fi) == str(g["fi_sha256"])
 
 
@@ -69,3 +72,20 @@ def test_fp64_oracle_tracks_fp32():
     a, b = run_oracle(case, "f32"), run_oracle(case, "f64")
     assert np.max(np.abs(a.u - b.u)) / np.max(np.abs(b.u)) < 1e-5
     assert np.max(np.abs(a.rho - b.rho)) < 1e-5
+
+
+def test_oracle_update_moving_boundaries_marks_like_initialize():
+    """update_moving_boundaries after initialize changes nothing (same marking, TYPE_T aside), and
+    stopping the lid clears every TYPE_MS mark."""
+    case = LC.CASE_BY_NAME["d3q19_srt_fp32_cavity_mb"]
+    o = oracle.Oracle(*case.shape, q=case.q, collision=case.collision, storage=case.storage, extensions=case.extensions, nu=case.nu)
+    f = case.fields()
+    o.rho[:], o.u[:], o.flags[:] = f["rho"], f["u"], f["flags"]
+    o.initialize()
+    marked = o.flags.copy()
+    o.update_moving_boundaries()
+    assert np.array_equal(o.flags, marked)
+    o.u[:] = 0.0
+    o.update_moving_boundaries()
+    assert np.count_nonzero((o.flags & 3) == 3) == 0
+    assert np.array_equal(o.flags, f["flags"])

@@ -21,18 +21,25 @@ def _harness(variant):
 
 VARIANTS = [(19, "srt", "fp32", ("eq", "ff", "vf")), (19, "trt", "fp16s", ("eq", "ff", "vf")), (19, "srt", "fp16c", ("eq",)),
             (27, "trt", "fp32", ("eq", "ff", "vf")), (27, "srt", "fp16s", ()),
-            (19, "srt", "fp32", ("sg",)), (19, "trt", "fp16s", ("eq", "sg")), (27, "trt", "fp32", ("eq", "ff", "sg", "vf"))]
+            (19, "srt", "fp32", ("sg",)), (19, "trt", "fp16s", ("eq", "sg")), (27, "trt", "fp32", ("eq", "ff", "sg", "vf")),
+            (19, "srt", "fp32", ("mb",)), (19, "trt", "fp16s", ("mb",)), (19, "trt", "fp16c", ("mb", "sg")),
+            (27, "trt", "fp32", ("eq", "ff", "mb", "vf"))]
 
 
 @pytest.mark.parametrize("variant", VARIANTS, ids=["_".join([str(v[0]), v[1], v[2], *v[3]]) for v in VARIANTS])
 def test_random_flags_and_fields(variant):
-    """Random fluid/solid/equilibrium cells, random rho/u/F, odd box: every kernel bit-identical."""
+    """Random fluid/solid/equilibrium cells, random rho/u/F, odd box: every kernel bit-identical.
+    MOVING_BOUNDARIES: solid cells keep their random velocities (moving walls); stale TYPE_MS and
+    TYPE_T cells are in the mix, and halfway the solids' velocities change and
+    update_moving_boundaries re-marks the cells next to them."""
     _harness(variant)
     q, col, st, ext = variant
+    mb = "mb" in ext
     Nx, Ny, Nz = 13, 9, 7
     N = Nx * Ny * Nz
     rng = np.random.default_rng(42)
-    flags = rng.choice(np.array([0, 0, 0, 0, 0x01, 0x02 if "eq" in ext else 0, 0x41], np.uint8), N)
+    mix = [0, 0, 0, 0, 0x01, 0x02 if "eq" in ext else 0, 0x41] + ([0x03, 0x04, 0x01] if mb else [])
+    flags = rng.choice(np.array(mix, np.uint8), N)
     rho = (1.0 + rng.normal(0, 0.01, N)).astype(np.float32)
     u = rng.normal(0, 0.03, 3 * N).astype(np.float32)
     F = rng.normal(0, 2e-4, 3 * N).astype(np.float32)
@@ -43,7 +50,16 @@ def test_random_flags_and_fields(variant):
         m.initialize()
         states = [m.fi.copy()]
         fx = 3e-5 if "vf" in ext else 0.0
+        states.append(m.flags.copy())
         for steps in (1, 4):
+            if mb and steps == 4:  # some walls stop, the others change speed
+                solid = (m.flags & 3) == 1
+                m.u[:N][solid] *= np.float32(0.5)
+                m.u[N:2 * N][solid & (np.arange(N) % 3 == 0)] = 0.0
+                m.u[:N][solid & (np.arange(N) % 5 == 0)] = 0.0
+                m.u[2 * N:][solid & (np.arange(N) % 5 == 0)] = 0.0
+                m.update_moving_boundaries()
+                states.append(m.flags.copy())
             m.run(steps, fx, -1e-5 if fx else 0.0, 2e-5 if fx else 0.0)
             m.update_fields(fx, -1e-5 if fx else 0.0, 2e-5 if fx else 0.0)
             states += [m.fi.copy(), m.rho.copy(), m.u.copy()]
