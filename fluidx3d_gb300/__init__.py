@@ -7,6 +7,7 @@ from .setups import TYPE_S, TYPE_E, TYPE_T, TYPE_F, TYPE_I, TYPE_G, TYPE_X, TYPE
 from ._capi import LBMError, relaxation_rate  # noqa: F401
 from .lbm import LBM, Field  # noqa: F401
 from .mesh import Mesh, read_stl, write_stl, ellipsoid_mesh, sphere_mesh  # noqa: F401
+from .units import Units, units  # noqa: F401
 
-__all__ = ["LBM", "Field", "LBMError", "Mesh", "read_stl", "write_stl", "ellipsoid_mesh", "sphere_mesh", "relaxation_rate",
+__all__ = ["LBM", "Field", "LBMError", "Mesh", "read_stl", "write_stl", "ellipsoid_mesh", "sphere_mesh", "relaxation_rate", "Units", "units",
            "TYPE_S", "TYPE_E", "TYPE_T", "TYPE_F", "TYPE_I", "TYPE_G", "TYPE_X", "TYPE_Y"]

@@ -14,7 +14,7 @@ LBM_OK = 0
 STATUS_NAMES = {1: "INVALID_ARGUMENT", 2: "OUT_OF_MEMORY", 3: "CUDA", 4: "NOT_INITIALIZED", 5: "UNSUPPORTED", 6: "NO_DEVICE", 7: "IO"}
 SRT, TRT = 0, 1
 FP32, FP16S, FP16C = 0, 1, 2
-EXT_VOLUME_FORCE, EXT_FORCE_FIELD, EXT_EQUILIBRIUM_BOUNDARIES, EXT_SUBGRID, EXT_MOVING_BOUNDARIES = 1, 2, 4, 8, 16
+EXT_VOLUME_FORCE, EXT_FORCE_FIELD, EXT_EQUILIBRIUM_BOUNDARIES, EXT_SUBGRID, EXT_MOVING_BOUNDARIES, EXT_UPDATE_FIELDS = 1, 2, 4, 8, 16, 32
 FIELD_RHO, FIELD_U, FIELD_FLAGS, FIELD_F, FIELD_FI = 0, 1, 2, 3, 4
 ARITH_AUTO, ARITH_EXACT, ARITH_FAST = 0, 1, 2
 ARITHMETICS = {"auto": ARITH_AUTO, "exact": ARITH_EXACT, "fast": ARITH_FAST}
@@ -23,7 +23,8 @@ COLLISIONS = {"srt": SRT, "trt": TRT}
 STORAGES = {"fp32": FP32, "fp16s": FP16S, "fp16c": FP16C}
 EXTENSIONS = {"volume_force": EXT_VOLUME_FORCE, "force_field": EXT_FORCE_FIELD, "equilibrium_boundaries": EXT_EQUILIBRIUM_BOUNDARIES,
               "subgrid": EXT_SUBGRID, "moving_boundaries": EXT_MOVING_BOUNDARIES, "vf": EXT_VOLUME_FORCE, "ff": EXT_FORCE_FIELD,
-              "eq": EXT_EQUILIBRIUM_BOUNDARIES, "sg": EXT_SUBGRID, "mb": EXT_MOVING_BOUNDARIES}
+              "update_fields": EXT_UPDATE_FIELDS, "eq": EXT_EQUILIBRIUM_BOUNDARIES, "sg": EXT_SUBGRID, "mb": EXT_MOVING_BOUNDARIES,
+              "uf": EXT_UPDATE_FIELDS}
 
 
 class LBMError(RuntimeError):

@@ -65,12 +65,14 @@ struct lbm_domain {
 	uint64_t t_last_update_fields = UINT64_MAX;
 	uint64_t t_last_force_field = UINT64_MAX;
 	bool initialized = false;
+	bool fused_fields = false; // LBM_EXT_UPDATE_FIELDS: every stream_collide writes rho/u
 
 	StepArgs args() const {
 		StepArgs a;
 		a.g = g; a.fi = fi; a.fi_dst = fi; a.rho = rho; a.u = u; a.flags = flags; a.F = F;
 		a.t = t; a.fx = cfg.fx; a.fy = cfg.fy; a.fz = cfg.fz; a.w = w;
 		a.err = err;
+		a.fields_out = fused_fields ? 1 : 0;
 		a.omw = rates.omw; a.c_tau = rates.c_tau; a.hp = rates.hp; a.hm = rates.hm; a.c_taup = rates.c_taup; a.c_taum = rates.c_taum;
 		return a;
 	}
@@ -143,6 +145,7 @@ int ensure_F(lbm_domain* d) {
 }
 
 int do_update_fields(lbm_domain* d) {
+	if(d->fused_fields) return LBM_OK; // the steps keep rho/u current (src/lbm.cpp:184-191 compiles to nothing with UPDATE_FIELDS)
 	if(d->t==d->t_last_update_fields) return LBM_OK;
 	const StepArgs a = d->args();
 	cudaError_t e;
@@ -251,6 +254,7 @@ uint32_t lbm_bytes_per_cell_device(const lbm_config* c) {
 uint32_t lbm_bandwidth_bytes_per_cell(const lbm_config* c) {
 	if(!c) return 0u;
 	uint32_t b = c->velocity_set*2u*(uint32_t)ddf_bytes(c->storage)+1u;
+	if(c->extensions&LBM_EXT_UPDATE_FIELDS) b += 16u; // rho, u (src/lbm.cpp:53-58)
 	if(c->extensions&LBM_EXT_FORCE_FIELD) b += 12u;
 	if(c->extensions&LBM_EXT_MOVING_BOUNDARIES) b += c->velocity_set-1u; // neighbour flags (src/lbm.cpp:62-64)
 	return b;
@@ -266,7 +270,7 @@ int lbm_domain_create(const lbm_config* c, lbm_domain** out) {
 	if(c->velocity_set!=19u&&c->velocity_set!=27u) return fail(LBM_ERR_INVALID_ARGUMENT, "velocity_set must be 19 or 27, got %u", c->velocity_set);
 	if(c->collision>LBM_TRT) return fail(LBM_ERR_INVALID_ARGUMENT, "collision must be LBM_SRT or LBM_TRT");
 	if(c->storage>LBM_FP16C) return fail(LBM_ERR_INVALID_ARGUMENT, "storage must be LBM_FP32, LBM_FP16S or LBM_FP16C");
-	if(c->extensions&~31u) return fail(LBM_ERR_INVALID_ARGUMENT, "unknown extension bits 0x%x", c->extensions&~31u);
+	if(c->extensions&~63u) return fail(LBM_ERR_INVALID_ARGUMENT, "unknown extension bits 0x%x", c->extensions&~63u);
 	if(c->arithmetic>LBM_ARITH_FAST) return fail(LBM_ERR_INVALID_ARGUMENT, "arithmetic must be LBM_ARITH_AUTO, LBM_ARITH_EXACT or LBM_ARITH_FAST");
 	if(!(c->nu>0.0f)) return fail(LBM_ERR_INVALID_ARGUMENT, c->nu==0.0f ? "Viscosity cannot be 0." : "Viscosity cannot be negative.");
 	if(!(c->extensions&LBM_EXT_VOLUME_FORCE)&&(c->fx!=0.0f||c->fy!=0.0f||c->fz!=0.0f))
@@ -299,6 +303,7 @@ int lbm_domain_create(const lbm_config* c, lbm_domain** out) {
 	if(c->extensions&LBM_EXT_SUBGRID) ext |= EXT_SG;
 	if(c->extensions&LBM_EXT_MOVING_BOUNDARIES) ext |= EXT_MB;
 	d->v.ext = ext;
+	d->fused_fields = (c->extensions&LBM_EXT_UPDATE_FIELDS)!=0u;
 	d->v.fast = c->arithmetic==LBM_ARITH_FAST || (c->arithmetic==LBM_ARITH_AUTO && c->storage!=LBM_FP32);
 	d->g.Nx = c->Nx; d->g.Ny = c->Ny; d->g.Nz = c->Nz; d->g.NxNy = c->Nx*c->Ny; d->g.N = N;
 	d->g.nx_inv = c->Nx==1u ? 0ull : (~0ull)/c->Nx+1ull; // ceil(2^64/Nx)
@@ -415,7 +420,7 @@ int lbm_initialize(lbm_domain* d) {
 	}
 	d->t = 0ull; // src/lbm.cpp:920
 	if(e!=cudaSuccess) return cuda_fail(e, "initialize");
-	d->t_last_update_fields = UINT64_MAX;
+	d->t_last_update_fields = d->fused_fields ? 0ull : UINT64_MAX; // src/lbm.cpp:261-266
 	d->t_last_force_field = UINT64_MAX;
 	d->initialized = true;
 	return LBM_OK;
@@ -429,6 +434,7 @@ int lbm_stream_collide(lbm_domain* d, const uint64_t steps) {
 		if(r!=LBM_OK) return r;
 		d->t++;
 	}
+	if(d->fused_fields) d->t_last_update_fields = d->t; // src/lbm.cpp:255-260
 	return LBM_OK;
 }
 
@@ -672,6 +678,7 @@ struct DeviceBuffer { // freed on scope exit
 int step_out_of_place(lbm_domain* d, const void* src, void* dst, const uint64_t t) {
 	StepArgs a = d->args();
 	a.t = t;
+	a.fields_out = 0; // recomputed states leave the fields of the forward run alone
 	const bool rows_ok = row_plan(d->v.q, d->v.storage, d->g.Nx, d->g.Ny, d->g.Nz).stages!=0u;
 	int path = d->path==PATH_ROWS && rows_ok ? PATH_ROWS : PATH_CELLS;
 	if(d->path==PATH_PAIRS||d->path==PATH_PIPE) {
@@ -820,7 +827,7 @@ extern "C" int lbm_run_adjoint(lbm_domain* d, const lbm_adjoint_config* cfg, dou
 		stats->forward_ms = forward_ms; stats->recompute_ms = recompute_ms; stats->adjoint_ms = adjoint_ms;
 		stats->workspace_bytes = (uint64_t)need; stats->levels = levels; stats->reserved = 0u;
 	}
-	d->t_last_update_fields = UINT64_MAX;
+	d->t_last_update_fields = d->fused_fields ? d->t : UINT64_MAX;
 	d->t_last_force_field = UINT64_MAX;
 	return LBM_OK;
 }

@@ -10,6 +10,8 @@
 //   k_update_force_field  src/kernel.cpp:1873-1884 update_force_field
 // MOVING_BOUNDARIES (EXT_MB) adds apply_moving_boundaries (src/kernel.cpp:1104-1113) to
 // stream_collide and update_fields and the TYPE_MS marking of initialize (src/kernel.cpp:1378-1387).
+// UPDATE_FIELDS (StepArgs::fields_out, a run-time switch) makes stream_collide write rho/u
+// (src/kernel.cpp:1565-1573), in every kernel through store_fields.
 #pragma once
 #include "lbm_scheme.cuh"
 #include "lbm_internal.h"
@@ -112,6 +114,18 @@ template<int Q, int EXT> __device__ __forceinline__ void cell_rho_u(const StepAr
 	shift_clamp<VF>(ux, uy, uz, rho, fx, fy, fz);
 }
 
+// UPDATE_FIELDS (src/kernel.cpp:1565-1573): the density and the (force-shifted, clamped) velocity a
+// cell collides with, written to rho/u; V = float2 writes cells n and n+1 (n even) as aligned pairs
+__device__ __forceinline__ void store_fields(const StepArgs& a, const uint64_t n, const float rho, const float ux, const float uy, const float uz) {
+	const uint64_t N = a.g.N;
+	a.rho[n] = rho; a.u[n] = ux; a.u[N+n] = uy; a.u[2ull*N+n] = uz;
+}
+__device__ __forceinline__ void store_fields(const StepArgs& a, const uint64_t n, const float2 rho, const float2 ux, const float2 uy, const float2 uz) {
+	const uint64_t N = a.g.N;
+	*reinterpret_cast<float2*>(a.rho+n) = rho; *reinterpret_cast<float2*>(a.u+n) = ux;
+	*reinterpret_cast<float2*>(a.u+N+n) = uy; *reinterpret_cast<float2*>(a.u+2ull*N+n) = uz;
+}
+
 // one cell step on registers: f in, f out (exact: real units; fast: storage units)
 // (SUBGRID: the cell's relaxation rate from the Smagorinsky-Lilly model, src/kernel.cpp:1579-1593)
 template<int Q, int ST, bool TRT, int EXT, bool FAST> __device__ __forceinline__ void cell_step(float* f, const StepArgs& a, const uint64_t n, const bool is_e) {
@@ -120,9 +134,11 @@ template<int Q, int ST, bool TRT, int EXT, bool FAST> __device__ __forceinline__
 	if constexpr(FAST) {
 		float rm1, inv;
 		cell_rho_u_fast<Q, EXT, ST>(a, n, f, is_e, rho, rm1, inv, ux, uy, uz, fx, fy, fz);
+		if(a.fields_out && !is_e) store_fields(a, n, __fmul_rn(rho, 1.0f/RawCodec<ST>::K), ux, uy, uz); // rho = R/K exactly
 		collide_fast<Q, TRT, VF, ST, SG>(f, rho, rm1, ux, uy, uz, fx, fy, fz, is_e, a);
 	} else {
 		cell_rho_u<Q, EXT>(a, n, f, is_e, rho, ux, uy, uz, fx, fy, fz);
+		if(a.fields_out && !is_e) store_fields(a, n, rho, ux, uy, uz);
 		if constexpr(SG) {
 			StepArgs b = a; // the same step with this cell's rates
 			b.w = subgrid_w_exact<Q>(f, eq_state(rho, ux, uy, uz), a.w);
@@ -225,6 +241,16 @@ template<int Q, int ST, typename T> __device__ __forceinline__ void store_pair(T
 	});
 }
 
+// UPDATE_FIELDS for a pair: both cells as aligned pairs, or each non-TYPE_E cell alone
+template<int ST> __device__ __forceinline__ void store_pair_fields(const StepArgs& a, const uint64_t n, const float2 R, const float2 ux, const float2 uy,
+                                                                   const float2 uz, const Bool2 is_e, const bool any_e) {
+	constexpr float k = 1.0f/RawCodec<ST>::K;
+	const float2 rho = v_mul(R, make_float2(k, k)); // exact: K is a power of two
+	if(!any_e) { store_fields(a, n, rho, ux, uy, uz); return; }
+	if(!is_e.x) store_fields(a, n, rho.x, ux.x, uy.x, uz.x);
+	if(!is_e.y) store_fields(a, n+1ull, rho.y, ux.y, uy.y, uz.y);
+}
+
 inline dim3 pair_grid(const GridDesc& g) { return dim3((g.NxNy/2u+BLOCK-1u)/BLOCK, g.Nz, 1u); }
 inline bool pairs_supported(const GridDesc& g) { return g.Nx%2u==0u && g.N<=0xFFFFFFFFull; }
 
@@ -260,6 +286,7 @@ template<int Q, int ST, bool TRT, int EXT> __global__ void __launch_bounds__(BLO
 	const bool any_e = is_e.x||is_e.y;
 	float2 R, Rm1, inv, ux, uy, uz, fx, fy, fz;
 	cell_rho_u_v<Q, EXT, ST, float2>(a, n, f, is_e, any_e, R, Rm1, inv, ux, uy, uz, fx, fy, fz);
+	if(a.fields_out) store_pair_fields<ST>(a, n, R, ux, uy, uz, is_e, any_e);
 	if(any_e) collide_v<Q, TRT, VF, ST, 2, float2, Bool2, (EXT&EXT_SG)!=0>(f, R, Rm1, ux, uy, uz, fx, fy, fz, is_e, a);
 	else collide_v<Q, TRT, VF, ST, 0, float2, Bool2, (EXT&EXT_SG)!=0>(f, R, Rm1, ux, uy, uz, fx, fy, fz, is_e, a);
 	store_pair<Q, ST>((T*)a.fi, g.N, sa, sb, odd, f);
@@ -426,6 +453,7 @@ template<int Q, int ST, bool TRT, int EXT, int S> __global__ void __launch_bound
 		const bool any_e = is_e.x||is_e.y;
 		float2 R, Rm1, inv, ux, uy, uz, fx, fy, fz;
 		cell_rho_u_v<Q, EXT, ST, float2>(a, n, f, is_e, any_e, R, Rm1, inv, ux, uy, uz, fx, fy, fz);
+		if(a.fields_out) store_pair_fields<ST>(a, n, R, ux, uy, uz, is_e, any_e);
 		if constexpr(FX3D_PIPE_REREAD!=0) { // read the staged values again instead of holding them through the moments
 			asm volatile("" ::: "memory");
 			read_pair<Q, ST>(w, f);

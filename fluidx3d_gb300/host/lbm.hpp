@@ -4,7 +4,8 @@
 //
 // The variant is chosen the way the reference chooses it, with macros defined before this header
 // is included (src/defines.hpp:5-29): D3Q19 (default) or D3Q27; SRT (default) or TRT; FP16S or
-// FP16C DDF storage (default FP32); VOLUME_FORCE, FORCE_FIELD, EQUILIBRIUM_BOUNDARIES, SUBGRID, MOVING_BOUNDARIES;
+// FP16C DDF storage (default FP32); VOLUME_FORCE, FORCE_FIELD, EQUILIBRIUM_BOUNDARIES, SUBGRID, MOVING_BOUNDARIES,
+// UPDATE_FIELDS;
 // and, new here,
 // EXACT_ARITHMETIC / FAST_ARITHMETIC (default: exact with FP32 storage, fast with FP16S/FP16C).
 //
@@ -18,6 +19,7 @@
 #include <iterator>
 #include <algorithm>
 #include <fstream>
+#include <filesystem>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -57,6 +59,70 @@ inline float3 operator+(const float3& a, const float3& b) { return float3(a.x+b.
 inline float3 operator-(const float3& a, const float3& b) { return float3(a.x-b.x, a.y-b.y, a.z-b.z); }
 inline float3 operator*(const float s, const float3& a) { return float3(s*a.x, s*a.y, s*a.z); }
 inline float3 operator/(const float3& a, const float s) { return float3(a.x/s, a.y/s, a.z/s); }
+inline float3 operator*(const float3& a, const float s) { return float3(a.x*s, a.y*s, a.z*s); }
+inline float3 operator-(const float3& a) { return float3(-a.x, -a.y, -a.z); }
+// 3x3 matrix, row-major (src/utilities.hpp float3x3); m*v sums each row left to right
+struct float3x3 {
+	float xx = 1.0f, xy = 0.0f, xz = 0.0f, yx = 0.0f, yy = 1.0f, yz = 0.0f, zx = 0.0f, zy = 0.0f, zz = 1.0f;
+	float3x3() = default;
+	explicit float3x3(const float s) : xx(s), xy(0.0f), xz(0.0f), yx(0.0f), yy(s), yz(0.0f), zx(0.0f), zy(0.0f), zz(s) {}
+	float3x3(const float xx, const float xy, const float xz, const float yx, const float yy, const float yz, const float zx, const float zy, const float zz)
+		: xx(xx), xy(xy), xz(xz), yx(yx), yy(yy), yz(yz), zx(zx), zy(zy), zz(zz) {}
+};
+inline float3 operator*(const float3x3& m, const float3& v) { return float3(m.xx*v.x+m.xy*v.y+m.xz*v.z, m.yx*v.x+m.yy*v.y+m.yz*v.z, m.zx*v.x+m.zy*v.y+m.zz*v.z); }
+
+// unit conversion lattice <-> SI (src/units.hpp:5-75); `units` is the program-wide instance, identity by default
+class Units {
+public:
+	float unit_m = 1.0f, unit_kg = 1.0f, unit_s = 1.0f;
+	void set_m_kg_s(const float x, const float u, const float rho, const float si_x, const float si_u, const float si_rho) {
+		unit_m = si_x/x;
+		unit_kg = si_rho/rho*(unit_m*unit_m*unit_m);
+		unit_s = u/si_u*unit_m;
+	}
+	void set_m_kg_s(const float m, const float kg, const float s) { unit_m = m; unit_kg = kg; unit_s = s; }
+	float x(const float si_x) const { return si_x/unit_m; }
+	float u(const float si_u) const { return si_u*unit_s/unit_m; }
+	float rho(const float si_rho) const { return si_rho*(unit_m*unit_m*unit_m)/unit_kg; }
+	float nu(const float si_nu) const { return si_nu*unit_s/(unit_m*unit_m); }
+	float F(const float si_F) const { return si_F*(unit_s*unit_s)/(unit_kg*unit_m); }
+	ulong t(const float si_t) const { return (ulong)std::fmax(si_t/unit_s+0.5f, 0.5f); }
+	float si_x(const float x) const { return x*unit_m; }
+	float si_t(const ulong t) const { return (float)t*unit_s; }
+	float si_u(const float u) const { return u*unit_m/unit_s; }
+	float si_rho(const float rho) const { return rho*unit_kg/(unit_m*unit_m*unit_m); }
+	float si_nu(const float nu) const { return nu*(unit_m*unit_m)/unit_s; }
+	float si_F(const float F) const { return F*unit_kg*unit_m/(unit_s*unit_s); }
+};
+inline Units units;
+
+// file names and folders (src/lbm.cpp:85-92, src/utilities.hpp:4197-4207)
+inline std::string create_file_extension(const std::string& filename, const std::string& extension) {
+	return filename.substr(0, filename.rfind('.'))+(extension.at(0)!='.' ? "." : "")+extension;
+}
+inline void create_folder(const std::string& path) {
+	const size_t slash = path.rfind('/');
+	if(slash==std::string::npos||slash==0u) return;
+	std::error_code ec;
+	std::filesystem::create_directories(path.substr(0u, slash), ec);
+}
+inline std::string get_exe_path() { // folder of the running executable, with a trailing '/'
+	std::error_code ec;
+	const std::filesystem::path p = std::filesystem::read_symlink("/proc/self/exe", ec);
+	return ec ? std::string("./") : p.parent_path().string()+"/";
+}
+inline std::string default_filename(const std::string& path, const std::string& name, const std::string& extension, const ulong t) {
+	std::string time = "00000000"+std::to_string(t);
+	time = time.substr(time.length()-9u, 9u);
+	return (path=="" ? get_exe_path()+"export/" : path)+create_file_extension((name=="" ? "file" : name)+"-"+time, extension);
+}
+template<typename T> inline T reverse_bytes(const T x) {
+	T r;
+	const unsigned char* a = reinterpret_cast<const unsigned char*>(&x);
+	unsigned char* b = reinterpret_cast<unsigned char*>(&r);
+	for(size_t i=0u; i<sizeof(T); i++) b[i] = a[sizeof(T)-1u-i];
+	return r;
+}
 inline float length(const float3& a) { return std::sqrt(a.x*a.x+a.y*a.y+a.z*a.z); }
 struct uint3 {
 	uint x = 0u, y = 0u, z = 0u;
@@ -84,25 +150,44 @@ struct Mesh {
 		for(uint i=0u; i<triangle_number; i++) { p0[i] += t; p1[i] += t; p2[i] += t; }
 		center += t; pmin += t; pmax += t;
 	}
+	float get_max_size() const { return std::fmax(std::fmax(pmax.x-pmin.x, pmax.y-pmin.y), pmax.z-pmin.z); }
+	float get_scale_for_box_fit(const float3& b) const { return std::fmin(std::fmin(b.x/(pmax.x-pmin.x), b.y/(pmax.y-pmin.y)), b.z/(pmax.z-pmin.z)); }
 };
 
-// binary STL file without rescaling (src/utilities.hpp:4530-4581 read_stl_raw with reposition=false, scale 1)
-inline Mesh* read_stl(const std::string& path) {
-	std::ifstream file(path, std::ios::in|std::ios::binary);
-	if(!file) throw lbm_error(LBM_ERR_INVALID_ARGUMENT, "File \""+path+"\" does not exist!");
+// binary STL file (src/utilities.hpp:4530-4581 read_stl_raw): vertices rotated, then rescaled (size 0:
+// fit box_size; size > 0: longest side = size; size < 0: factor -size) and, with reposition, centred
+// on `center`
+inline Mesh* read_stl_raw(const std::string& path, const bool reposition, const float3& box_size, const float3& center, const float3x3& rotation, const float size) {
+	const std::string filename = create_file_extension(path, ".stl");
+	std::ifstream file(filename, std::ios::in|std::ios::binary);
+	if(!file) throw lbm_error(LBM_ERR_INVALID_ARGUMENT, "File \""+filename+"\" does not exist!");
 	std::vector<char> data((std::istreambuf_iterator<char>(file)), std::istreambuf_iterator<char>());
-	if(data.size()<84u) throw lbm_error(LBM_ERR_INVALID_ARGUMENT, "File \""+path+"\" is corrupt!");
+	if(data.size()<84u) throw lbm_error(LBM_ERR_INVALID_ARGUMENT, "File \""+filename+"\" is corrupt!");
 	uint T = 0u;
 	std::memcpy(&T, data.data()+80, 4);
-	if(T==0u||data.size()!=84u+50u*(size_t)T) throw lbm_error(LBM_ERR_INVALID_ARGUMENT, "File \""+path+"\" is corrupt or unsupported! Only binary .stl files are supported.");
-	Mesh* mesh = new Mesh(T, float3(0.0f));
+	if(T==0u||data.size()!=84u+50u*(size_t)T) throw lbm_error(LBM_ERR_INVALID_ARGUMENT, "File \""+filename+"\" is corrupt or unsupported! Only binary .stl files are supported.");
+	Mesh* mesh = new Mesh(T, center);
 	for(uint i=0u; i<T; i++) {
 		float v[12];
 		std::memcpy(v, data.data()+84u+50u*(size_t)i, 48);
-		mesh->p0[i] = float3(v[3], v[4], v[5]); mesh->p1[i] = float3(v[6], v[7], v[8]); mesh->p2[i] = float3(v[9], v[10], v[11]);
+		mesh->p0[i] = rotation*float3(v[3], v[4], v[5]); mesh->p1[i] = rotation*float3(v[6], v[7], v[8]); mesh->p2[i] = rotation*float3(v[9], v[10], v[11]);
+	}
+	mesh->find_bounds();
+	const float scale = size==0.0f ? mesh->get_scale_for_box_fit(box_size) : size>0.0f ? size/mesh->get_max_size() : -size;
+	const float3 offset = reposition ? -(0.5f*(mesh->pmin+mesh->pmax)) : float3(0.0f);
+	for(uint i=0u; i<T; i++) {
+		mesh->p0[i] = center+scale*(offset+mesh->p0[i]);
+		mesh->p1[i] = center+scale*(offset+mesh->p1[i]);
+		mesh->p2[i] = center+scale*(offset+mesh->p2[i]);
 	}
 	mesh->find_bounds();
 	return mesh;
+}
+inline Mesh* read_stl(const std::string& path, const float3& box_size, const float3& center, const float3x3& rotation, const float size) { return read_stl_raw(path, true, box_size, center, rotation, size); }
+inline Mesh* read_stl(const std::string& path, const float3& box_size, const float3& center, const float size) { return read_stl_raw(path, true, box_size, center, float3x3(1.0f), size); }
+// no rescaling or repositioning: vertices rotated, scaled by |scale| and shifted by offset (file coordinates are lattice coordinates by default)
+inline Mesh* read_stl(const std::string& path, const float scale=1.0f, const float3x3& rotation=float3x3(1.0f), const float3& offset=float3(0.0f)) {
+	return read_stl_raw(path, false, float3(1.0f), offset, rotation, -std::fabs(scale));
 }
 
 // the variant the including setup selected with the reference's macros
@@ -141,6 +226,9 @@ inline lbm_config lbm_config_from_defines(const uint Nx, const uint Ny, const ui
 #endif
 #if defined(SUBGRID)
 	c.extensions |= LBM_EXT_SUBGRID;
+#endif
+#if defined(UPDATE_FIELDS)
+	c.extensions |= LBM_EXT_UPDATE_FIELDS;
 #endif
 	c.device = -1;
 	c.nu = nu; c.fx = fx; c.fy = fy; c.fz = fz;
@@ -197,6 +285,43 @@ public:
 		void reset(const T value=(T)0) { std::fill(data.begin(), data.end(), value); }
 		void read_from_device() { lbm_check(lbm_read_field(lbm->domain, field, data.data(), capacity())); } // updates rho/u first when stale
 		void write_to_device() { lbm_check(lbm_write_field(lbm->domain, field, data.data(), capacity())); }
+		// binary legacy VTK (src/lbm.hpp:298-340, 401-407), the host copy or straight from the device
+		std::string name() const { return field==LBM_FIELD_RHO ? "rho" : field==LBM_FIELD_U ? "u" : field==LBM_FIELD_F ? "F" : "flags"; }
+		float si_factor(const bool si) const {
+			if(!si) return 1.0f;
+			return field==LBM_FIELD_RHO ? units.si_rho(1.0f) : field==LBM_FIELD_U ? units.si_u(1.0f) : field==LBM_FIELD_F ? units.si_F(1.0f) : 1.0f;
+		}
+		void write_host_to_vtk(const std::string& path="", const bool convert_to_si_units=true) const {
+			const std::string filename = create_file_extension(default_filename(path, name(), ".vtk", lbm->get_t()), ".vtk");
+			const float spacing = convert_to_si_units ? units.si_x(1.0f) : 1.0f;
+			const float factor = si_factor(convert_to_si_units);
+			const float3 origin = spacing*float3(0.5f-0.5f*(float)lbm->Nx, 0.5f-0.5f*(float)lbm->Ny, 0.5f-0.5f*(float)lbm->Nz);
+			const std::string header = "# vtk DataFile Version 3.0\nFluidX3D "+filename.substr(filename.rfind('/')+1)+"\nBINARY\nDATASET STRUCTURED_POINTS\n"
+				"DIMENSIONS "+std::to_string(lbm->Nx)+" "+std::to_string(lbm->Ny)+" "+std::to_string(lbm->Nz)+"\n"
+				"ORIGIN "+std::to_string(origin.x)+" "+std::to_string(origin.y)+" "+std::to_string(origin.z)+"\n"
+				"SPACING "+std::to_string(spacing)+" "+std::to_string(spacing)+" "+std::to_string(spacing)+"\n"
+				"POINT_DATA "+std::to_string(N)+"\n"
+				"SCALARS data "+std::string(sizeof(T)==1u ? "unsigned_char" : "float")+" "+std::to_string(d)+"\nLOOKUP_TABLE default\n";
+			create_folder(filename);
+			std::ofstream file(filename, std::ios::out|std::ios::binary);
+			if(!file) throw lbm_error(LBM_ERR_IO, "File \""+filename+"\" cannot be written");
+			file.write(header.c_str(), (std::streamsize)header.length());
+			std::vector<T> chunk;
+			const ulong block = 1ull<<20;
+			for(ulong i0=0ull; i0<N; i0+=block) {
+				const ulong n1 = i0+block<N ? i0+block : N;
+				chunk.resize((size_t)(n1-i0)*d);
+				for(ulong i=i0; i<n1; i++) for(uint c=0u; c<d; c++) {
+					const T v = data[i+(ulong)c*N];
+					chunk[(size_t)(i-i0)*d+c] = sizeof(T)==1u ? v : reverse_bytes((T)(factor*v));
+				}
+				file.write((const char*)chunk.data(), (std::streamsize)(chunk.size()*sizeof(T)));
+			}
+		}
+		void write_device_to_vtk(const std::string& path="", const bool convert_to_si_units=true) const {
+			const std::string filename = create_file_extension(default_filename(path, name(), ".vtk", lbm->get_t()), ".vtk");
+			lbm_check(lbm_write_vtk(lbm->domain, field, filename.c_str(), convert_to_si_units ? units.si_x(1.0f) : 1.0f, si_factor(convert_to_si_units)));
+		}
 	};
 
 	Memory_Container<float> rho, u, F;
@@ -270,6 +395,33 @@ public:
 		const float rv[3] = {rotational_velocity.x, rotational_velocity.y, rotational_velocity.z};
 		lbm_check(lbm_voxelize_mesh(domain, &mesh->p0[0].x, &mesh->p1[0].x, &mesh->p2[0].x, mesh->triangle_number, flag, c, lv, rv));
 		if(!initialized) { flags.read_from_device(); u.read_from_device(); }
+	}
+	void write_mesh_to_vtk(const Mesh* mesh, const std::string& path="", const bool convert_to_si_units=true) const { // src/lbm.cpp:1094-1129
+		const std::string filename = default_filename(path, "mesh", ".vtk", get_t());
+		const uint T = mesh->triangle_number;
+		const std::string header_1 = "# vtk DataFile Version 3.0\nFluidX3D "+filename.substr(filename.rfind('/')+1)+"\nBINARY\nDATASET POLYDATA\nPOINTS "+std::to_string(3u*T)+" float\n";
+		const std::string header_2 = "POLYGONS "+std::to_string(T)+" "+std::to_string(4u*T)+"\n";
+		const float spacing = convert_to_si_units ? units.si_x(1.0f) : 1.0f;
+		const float3 offset = center();
+		std::vector<float> points(9u*(size_t)T);
+		std::vector<int> triangles(4u*(size_t)T);
+		for(uint i=0u; i<T; i++) {
+			const float3* p[3] = {&mesh->p0[i], &mesh->p1[i], &mesh->p2[i]};
+			for(uint k=0u; k<3u; k++) {
+				points[9u*(size_t)i+3u*k   ] = reverse_bytes(spacing*(p[k]->x-offset.x));
+				points[9u*(size_t)i+3u*k+1u] = reverse_bytes(spacing*(p[k]->y-offset.y));
+				points[9u*(size_t)i+3u*k+2u] = reverse_bytes(spacing*(p[k]->z-offset.z));
+			}
+			triangles[4u*(size_t)i] = reverse_bytes(3);
+			for(uint k=0u; k<3u; k++) triangles[4u*(size_t)i+1u+k] = reverse_bytes(3*(int)i+(int)k);
+		}
+		create_folder(filename);
+		std::ofstream file(filename, std::ios::out|std::ios::binary);
+		if(!file) throw lbm_error(LBM_ERR_IO, "File \""+filename+"\" cannot be written");
+		file.write(header_1.c_str(), (std::streamsize)header_1.length());
+		file.write((const char*)points.data(), (std::streamsize)(4u*9u*(size_t)T));
+		file.write(header_2.c_str(), (std::streamsize)header_2.length());
+		file.write((const char*)triangles.data(), (std::streamsize)(4u*4u*(size_t)T));
 	}
 	void unvoxelize_mesh_on_device(const Mesh* mesh, const uchar flag=TYPE_S) {
 		const float lo[3] = {mesh->pmin.x, mesh->pmin.y, mesh->pmin.z}, hi[3] = {mesh->pmax.x, mesh->pmax.y, mesh->pmax.z};

@@ -23,6 +23,8 @@ import ctypes
 import numpy as np
 
 from . import _capi as C
+from . import vtk as _vtk
+from .units import units
 from .setups import TYPE_S, TYPE_E, TYPE_T, TYPE_F, TYPE_I, TYPE_G, TYPE_X, TYPE_Y  # noqa: F401
 
 
@@ -33,8 +35,11 @@ class Field:
     for 3-component fields; indexing the Field indexes ``data``.
     """
 
+    NAMES = {C.FIELD_RHO: "rho", C.FIELD_U: "u", C.FIELD_FLAGS: "flags", C.FIELD_F: "F"}
+
     def __init__(self, lbm: "LBM", field_id: int, dims: int, dtype, fill):
         self.lbm, self.field_id, self.dims = lbm, field_id, dims
+        self.name = self.NAMES.get(field_id, "")
         self.data = np.full(lbm.get_N() * dims, fill, dtype=dtype)
         N = lbm.get_N()
         if dims == 3:
@@ -64,6 +69,29 @@ class Field:
 
     def write_to_device(self):
         self.lbm._check(C.load().lbm_write_field(self.lbm._d, self.field_id, self.data.ctypes.data, self.data.nbytes))
+
+    # ------------------------------------------------------------------ VTK export (src/lbm.hpp:298-340, 401-407)
+    def _vtk_units(self, convert_to_si_units):
+        if not convert_to_si_units:
+            return 1.0, 1.0
+        scale = {"rho": units.si_rho(1.0), "u": units.si_u(1.0), "F": units.si_F(1.0)}.get(self.name, 1.0)
+        return float(units.si_x(1.0)), float(scale)
+
+    def write_host_to_vtk(self, path="", convert_to_si_units=True):
+        """Writes the host copy as <path><name>-<t>.vtk (binary legacy VTK, the reference's format);
+        returns the file name. With convert_to_si_units, values and spacing go through ``units``."""
+        spacing, scale = self._vtk_units(convert_to_si_units)
+        fn = _vtk.default_filename(path, self.name, ".vtk", self.lbm.get_t())
+        return _vtk.write_field_vtk(fn, self.data, (self.lbm.get_Nx(), self.lbm.get_Ny(), self.lbm.get_Nz()), self.dims, spacing, scale)
+
+    def write_device_to_vtk(self, path="", convert_to_si_units=True):
+        """The same file straight from the device field: the GPU scales, interleaves and byte-swaps
+        the values chunk by chunk while the previous chunk is written (lbm_write_vtk); the host copy
+        is left as it is."""
+        spacing, scale = self._vtk_units(convert_to_si_units)
+        fn = _vtk.create_file_extension(_vtk.default_filename(path, self.name, ".vtk", self.lbm.get_t()), ".vtk")
+        self.lbm._check(C.load().lbm_write_vtk(self.lbm._d, self.field_id, fn.encode(), spacing, scale))
+        return fn
 
 
 def _ext_bits(extensions) -> int:
@@ -222,6 +250,12 @@ class LBM:
         if not self.initialized:  # host copies follow the device, so host-side set-up can continue
             self.flags.read_from_device()
             self.u.read_from_device()
+
+    def write_mesh_to_vtk(self, mesh, path="", convert_to_si_units=True):
+        """src/lbm.cpp:1094-1129: the mesh as <path>mesh-<t>.vtk, centred on the box (POLYDATA)."""
+        spacing = float(units.si_x(1.0)) if convert_to_si_units else 1.0
+        fn = _vtk.default_filename(path, "mesh", ".vtk", self.get_t())
+        return _vtk.write_mesh_vtk(fn, mesh, self.center(), spacing)
 
     def unvoxelize_mesh_on_device(self, mesh, flag=TYPE_S):
         lo = (ctypes.c_float * 3)(*np.asarray(mesh.pmin, np.float32))

@@ -63,7 +63,10 @@ def read_stl(path, box_size=None, center=None, rotation=None, size=0.0, repositi
     rec = np.frombuffer(data, dtype=np.dtype([("n", "<f4", 3), ("v", "<f4", (3, 3)), ("attr", "<u2")]), count=T, offset=84)
     v = rec["v"].astype(np.float32)
     R = np.eye(3, dtype=np.float32) if rotation is None else np.asarray(rotation, np.float32)
-    p0, p1, p2 = v[:, 0] @ R.T, v[:, 1] @ R.T, v[:, 2] @ R.T
+
+    def rot(q):  # float3x3*float3 in FP32, each row summed left to right
+        return np.stack([(R[r, 0] * q[:, 0] + R[r, 1] * q[:, 1]) + R[r, 2] * q[:, 2] for r in range(3)], axis=1).astype(np.float32)
+    p0, p1, p2 = rot(v[:, 0]), rot(v[:, 1]), rot(v[:, 2])
     allp = np.concatenate([p0, p1, p2])
     pmin, pmax = allp.min(axis=0), allp.max(axis=0)
     box = np.asarray(box_size if box_size is not None else (1.0, 1.0, 1.0), np.float32)

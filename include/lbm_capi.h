@@ -48,8 +48,12 @@ enum {
 	LBM_EXT_FORCE_FIELD = 2,           /* FORCE_FIELD: per-cell force F added to (fx,fy,fz) */
 	LBM_EXT_EQUILIBRIUM_BOUNDARIES = 4, /* EQUILIBRIUM_BOUNDARIES: TYPE_E cells held at their rho/u */
 	LBM_EXT_SUBGRID = 8,               /* SUBGRID: Smagorinsky-Lilly relaxation rate per cell (src/kernel.cpp:1579-1593); not with lbm_run_adjoint */
-	LBM_EXT_MOVING_BOUNDARIES = 16     /* MOVING_BOUNDARIES: TYPE_S cells with u != 0 are moving walls for their TYPE_MS
+	LBM_EXT_MOVING_BOUNDARIES = 16,    /* MOVING_BOUNDARIES: TYPE_S cells with u != 0 are moving walls for their TYPE_MS
 	                                    * neighbours (src/kernel.cpp:1104-1113, 1378-1387, 1431-1450); not with lbm_run_adjoint */
+	LBM_EXT_UPDATE_FIELDS = 32         /* UPDATE_FIELDS: every stream_collide writes the rho/u each cell collides with
+	                                    * (src/kernel.cpp:1565-1573; +16 B per cell and step), so reads of rho/u run no
+	                                    * update_fields (which becomes a no-op, src/lbm.cpp:184-191); the fields after a
+	                                    * step are those of the state the step started from, as in the reference */
 };
 /* arithmetic of the collision. EXACT evaluates the reference's FP32 operation order with IEEE
  * rounding at every step: bit-identical to the reference's kernel text evaluated on a CPU. FAST

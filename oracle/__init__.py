@@ -24,7 +24,7 @@ LIB = os.path.join(BUILD, "liblbm_oracle.so")
 REF_DIR = os.path.join(HERE, "_ref")
 
 STORAGE = {"fp32": 0, "fp16s": 1, "fp16c": 2}
-EXT_BITS = {"vf": 1, "ff": 2, "eq": 4, "sg": 8, "mb": 16}
+EXT_BITS = {"vf": 1, "ff": 2, "eq": 4, "sg": 8, "mb": 16, "uf": 32}
 
 
 def build_oracle(force: bool = False) -> str:

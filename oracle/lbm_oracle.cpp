@@ -12,6 +12,7 @@
 //   initialize                       src/kernel.cpp:1358-1430
 //   stream_collide (SRT/TRT, TYPE_S, TYPE_E, VOLUME_FORCE, FORCE_FIELD, SUBGRID)  src/kernel.cpp:1454-1636
 //   apply_moving_boundaries          src/kernel.cpp:1104-1113
+//   UPDATE_FIELDS (rho/u written by stream_collide)  src/kernel.cpp:1565-1573
 //   update_moving_boundaries         src/kernel.cpp:1431-1450
 //   update_fields                    src/kernel.cpp:1794-1870
 //   update_force_field               src/kernel.cpp:1873-1884
@@ -42,7 +43,7 @@ typedef uint32_t u32;
 typedef uint64_t u64;
 
 enum { ST_FP32 = 0, ST_FP16S = 1, ST_FP16C = 2 };
-enum { EXT_VOLUME_FORCE = 1, EXT_FORCE_FIELD = 2, EXT_EQUILIBRIUM_BOUNDARIES = 4, EXT_SUBGRID = 8, EXT_MOVING_BOUNDARIES = 16 };
+enum { EXT_VOLUME_FORCE = 1, EXT_FORCE_FIELD = 2, EXT_EQUILIBRIUM_BOUNDARIES = 4, EXT_SUBGRID = 8, EXT_MOVING_BOUNDARIES = 16, EXT_UPDATE_FIELDS = 32 };
 enum { T_S = 0x01, T_E = 0x02, T_T = 0x04, T_BO = 0x03, T_MS = 0x03, T_G = 0x20, T_SU = 0x38, T_XY = 0xC0 };
 
 extern "C" struct OracleConfig {
@@ -354,11 +355,11 @@ template<typename real> static void collide_cell(real* fhn, const real rhon, con
 	}
 }
 
-template<typename real> static int stream_collide_t(const OracleConfig* c, void* fi, const real* rho, const real* u, const u8* flags, const u64 t,
+template<typename real> static int stream_collide_t(const OracleConfig* c, void* fi, real* rho, real* u, const u8* flags, const u64 t,
                                                     const real fx, const real fy, const real fz, const real* F) {
 	const Grid G(c); const u32 q = c->q;
 	const bool eq = (c->ext&EXT_EQUILIBRIUM_BOUNDARIES)!=0u, ff = (c->ext&EXT_FORCE_FIELD)!=0u, vf = (c->ext&EXT_VOLUME_FORCE)!=0u;
-	const bool mb = (c->ext&EXT_MOVING_BOUNDARIES)!=0u;
+	const bool mb = (c->ext&EXT_MOVING_BOUNDARIES)!=0u, uf = (c->ext&EXT_UPDATE_FIELDS)!=0u;
 	parallel_cells(G.N, c->threads, [&](const u64 n) {
 		const u8 flagsn_bo = flags[n]&T_BO;
 		if(flagsn_bo==T_S||(flags[n]&T_SU)==T_G) return; // solid (implicit bounce-back through Esoteric-Pull) or gas: nothing
@@ -373,6 +374,7 @@ template<typename real> static int stream_collide_t(const OracleConfig* c, void*
 		real fxn = fx, fyn = fy, fzn = fz;
 		if(ff) { fxn += F[n]; fyn += F[G.N+n]; fzn += F[2ull*G.N+n]; }
 		shift_clamp<real>(uxn, uyn, uzn, rhon, fxn, fyn, fzn, vf);
+		if(uf && !is_e) { rho[n] = rhon; u[n] = uxn; u[G.N+n] = uyn; u[2ull*G.N+n] = uzn; } // UPDATE_FIELDS: the fields the cell collides with
 		collide_cell<real>(fhn, rhon, uxn, uyn, uzn, fxn, fyn, fzn, is_e, c);
 		store_f<real>(n, fhn, fi, j, t, q, G.N, c->storage);
 	});
@@ -561,19 +563,19 @@ float oracle_kernel_w(const float nu) {
 int oracle_initialize_f32(const OracleConfig* c, void* fi, float* rho, float* u, u8* flags) { return valid(c) ? initialize_t<float>(c, fi, rho, u, flags) : -1; }
 int oracle_initialize_f64(const OracleConfig* c, double* fi, double* rho, double* u, u8* flags) { return valid(c) ? initialize_t<double>(c, fi, rho, u, flags) : -1; }
 
-int oracle_stream_collide_f32(const OracleConfig* c, void* fi, const float* rho, const float* u, const u8* flags, const u64 t, const float fx, const float fy, const float fz, const float* F) {
+int oracle_stream_collide_f32(const OracleConfig* c, void* fi, float* rho, float* u, const u8* flags, const u64 t, const float fx, const float fy, const float fz, const float* F) {
 	return valid(c) ? stream_collide_t<float>(c, fi, rho, u, flags, t, fx, fy, fz, F) : -1;
 }
-int oracle_stream_collide_f64(const OracleConfig* c, double* fi, const double* rho, const double* u, const u8* flags, const u64 t, const double fx, const double fy, const double fz, const double* F) {
+int oracle_stream_collide_f64(const OracleConfig* c, double* fi, double* rho, double* u, const u8* flags, const u64 t, const double fx, const double fy, const double fz, const double* F) {
 	return valid(c) ? stream_collide_t<double>(c, fi, rho, u, flags, t, fx, fy, fz, F) : -1;
 }
 // steps consecutive time steps t0, t0+1, ... (the reference's LBM::run loop, src/lbm.cpp:955-975)
-int oracle_run_f32(const OracleConfig* c, void* fi, const float* rho, const float* u, const u8* flags, const u64 t0, const u64 steps, const float fx, const float fy, const float fz, const float* F) {
+int oracle_run_f32(const OracleConfig* c, void* fi, float* rho, float* u, const u8* flags, const u64 t0, const u64 steps, const float fx, const float fy, const float fz, const float* F) {
 	if(!valid(c)) return -1;
 	for(u64 s=0ull; s<steps; s++) stream_collide_t<float>(c, fi, rho, u, flags, t0+s, fx, fy, fz, F);
 	return 0;
 }
-int oracle_run_f64(const OracleConfig* c, double* fi, const double* rho, const double* u, const u8* flags, const u64 t0, const u64 steps, const double fx, const double fy, const double fz, const double* F) {
+int oracle_run_f64(const OracleConfig* c, double* fi, double* rho, double* u, const u8* flags, const u64 t0, const u64 steps, const double fx, const double fy, const double fz, const double* F) {
 	if(!valid(c)) return -1;
 	for(u64 s=0ull; s<steps; s++) stream_collide_t<double>(c, fi, rho, u, flags, t0+s, fx, fy, fz, F);
 	return 0;
@@ -822,12 +824,13 @@ extern "C" {
 double oracle_objective_f64(const OracleConfig* c, const double* f0, const u8* flags, const double* rho_p, const double* u_p, const double* F,
                             const double fx, const double fy, const double fz, const u64 steps, const OracleObjective* obj) {
 	const Grid G(c);
+	OracleConfig cf = *c; cf.ext &= ~(u32)EXT_UPDATE_FIELDS; // the forward steps leave rho/u alone (they are inputs here)
 	std::vector<double> f(f0, f0+(size_t)c->q*G.N);
 	double J = 0.0;
 	for(u64 t=0ull; t<=steps; t++) {
 		const double wgt = obj_weight(obj, G, flags, c, t);
 		if(wgt!=0.0) J += objective_state_f64(c, obj, f.data(), flags, rho_p, u_p, F, fx, fy, fz, t, wgt, nullptr, nullptr);
-		if(t<steps) stream_collide_t<double>(c, f.data(), rho_p, u_p, flags, t, fx, fy, fz, F);
+		if(t<steps) stream_collide_t<double>(&cf, f.data(), const_cast<double*>(rho_p), const_cast<double*>(u_p), flags, t, fx, fy, fz, F);
 	}
 	return J;
 }
@@ -839,6 +842,7 @@ int oracle_adjoint_f64(const OracleConfig* c, const double* f0, const u8* flags,
                        double* J_out, double* grad) {
 	if(!valid(c)||interval==0ull) return -1;
 	const Grid G(c);
+	OracleConfig cf = *c; cf.ext &= ~(u32)EXT_UPDATE_FIELDS; // the forward steps leave rho/u alone (they are inputs here)
 	const size_t S = (size_t)c->q*G.N;
 	std::vector<std::vector<double>> snaps;
 	std::vector<double> f(f0, f0+S);
@@ -847,7 +851,7 @@ int oracle_adjoint_f64(const OracleConfig* c, const double* f0, const u8* flags,
 		if(t%interval==0ull && t<steps) snaps.push_back(f);
 		const double wgt = obj_weight(obj, G, flags, c, t);
 		if(wgt!=0.0) J += objective_state_f64(c, obj, f.data(), flags, rho_p, u_p, F, fx, fy, fz, t, wgt, nullptr, nullptr);
-		if(t<steps) stream_collide_t<double>(c, f.data(), rho_p, u_p, flags, t, fx, fy, fz, F);
+		if(t<steps) stream_collide_t<double>(&cf, f.data(), const_cast<double*>(rho_p), const_cast<double*>(u_p), flags, t, fx, fy, fz, F);
 	}
 	std::vector<double> lambda(S, 0.0);
 	for(size_t i=0u; i<3u*G.N; i++) grad[i] = 0.0;
@@ -859,7 +863,7 @@ int oracle_adjoint_f64(const OracleConfig* c, const double* f0, const u8* flags,
 		std::vector<double> w = snaps[(size_t)s];
 		for(u64 k=k0; k<k1; k++) {
 			seg[(size_t)(k-k0)] = w;
-			if(k+1ull<k1) stream_collide_t<double>(c, w.data(), rho_p, u_p, flags, k, fx, fy, fz, F);
+			if(k+1ull<k1) stream_collide_t<double>(&cf, w.data(), const_cast<double*>(rho_p), const_cast<double*>(u_p), flags, k, fx, fy, fz, F);
 		}
 		for(u64 k=k1; k-->k0;) {
 			const std::vector<double>& fk = seg[(size_t)(k-k0)];

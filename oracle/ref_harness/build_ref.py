@@ -73,7 +73,8 @@ def _defines(q: int, collision: str, storage: str, extensions: tuple[str, ...]) 
     else:
         lines += ["#define fpxx float", "#define fpxx_copy float",
                   "#define load(p,o) (p)[o]", "#define store(p,o,x) (p)[o]=(x)"]
-    ext_macro = {"vf": "VOLUME_FORCE", "ff": "FORCE_FIELD", "eq": "EQUILIBRIUM_BOUNDARIES", "sg": "SUBGRID", "mb": "MOVING_BOUNDARIES"}
+    ext_macro = {"vf": "VOLUME_FORCE", "ff": "FORCE_FIELD", "eq": "EQUILIBRIUM_BOUNDARIES", "sg": "SUBGRID", "mb": "MOVING_BOUNDARIES",
+                 "uf": "UPDATE_FIELDS"}
     lines += [f"#define {ext_macro[e]}" for e in extensions]
     return "\n".join(lines) + "\n"
 
@@ -148,6 +149,9 @@ DEFAULT_VARIANTS = [
     (19, "trt", "fp16s", ("mb",)),
     (19, "trt", "fp16c", ("mb", "sg")),
     (27, "trt", "fp32", ("eq", "ff", "mb", "vf")),
+    (19, "srt", "fp32", ("uf",)),
+    (19, "trt", "fp16s", ("eq", "ff", "uf", "vf")),
+    (27, "trt", "fp16c", ("eq", "mb", "uf")),
 ]
 
 

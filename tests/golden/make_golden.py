@@ -45,7 +45,7 @@ def run_case(case, threads=None):
     h.rho[:], h.u[:], h.flags[:], h.F[:] = f["rho"], f["u"], f["flags"], f["F"]
     h.initialize()
     h.run(case.steps, *case.force)
-    h.update_fields(*case.force)
+    case.settle_fields(h)
     if "ff" in case.extensions:
         h.update_force_field()
     return h

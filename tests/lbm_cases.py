@@ -56,6 +56,13 @@ class Case:
     def force(self):
         return (self.fx, 0.0, 0.0)
 
+    def settle_fields(self, m):
+        """rho/u as a read of the fields gives them: update_fields, except with UPDATE_FIELDS, where
+        the steps wrote them (the fields of the state each step started from) and update_fields is
+        compiled out (src/lbm.cpp:184-191)."""
+        if "uf" not in self.extensions:
+            m.update_fields(*self.force)
+
 
 CASES = [
     Case("d3q19_srt_fp32_tgv", 19, "srt", "fp32"),
@@ -78,6 +85,9 @@ CASES = [
     Case("d3q19_trt_fp16c_couette_mb_sg", 19, "trt", "fp16c", ("mb", "sg"), "couette", (16, 16, 12), nu=0.01),
     Case("d3q27_trt_fp32_channel_eq_ff_mb_vf", 27, "trt", "fp32", ("eq", "ff", "mb", "vf"), "channel", fx=1e-5,
          extra={"sphere_u": (0.0, 0.02, -0.01)}),
+    Case("d3q19_srt_fp32_tgv_uf", 19, "srt", "fp32", ("uf",)),
+    Case("d3q19_trt_fp16s_channel_eq_ff_uf_vf", 19, "trt", "fp16s", ("eq", "ff", "uf", "vf"), "channel", fx=1e-5),
+    Case("d3q27_trt_fp16c_couette_eq_mb_uf", 27, "trt", "fp16c", ("eq", "mb", "uf"), "couette", (16, 16, 12)),
 ]
 CASE_BY_NAME = {c.name: c for c in CASES}
 

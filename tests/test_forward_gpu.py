@@ -79,7 +79,7 @@ def test_gpu_matches_oracle_step_by_step(case, gpu, path):
             lbm.flags.read_from_device()
             assert np.array_equal(lbm.flags.data, o.flags) and np.count_nonzero((o.flags & 3) == 3) > 0
         # reading u after initialize runs update_fields first, as the reference's lazy read does
-        o.update_fields(*case.force)
+        case.settle_fields(o)
         lbm.u.read_from_device()
         assert np.array_equal(lbm.u.data, o.u)
         for steps in (1, 1, 3):
@@ -87,7 +87,7 @@ def test_gpu_matches_oracle_step_by_step(case, gpu, path):
             lbm.run(steps)
             assert lbm.get_t() == o.t
             assert np.array_equal(lbm.read_ddfs(), o.fi), f"DDFs differ at t={o.t}"
-            o.update_fields(*case.force)
+            case.settle_fields(o)
             lbm.rho.read_from_device()
             lbm.u.read_from_device()
             assert np.array_equal(lbm.rho.data, o.rho) and np.array_equal(lbm.u.data, o.u)

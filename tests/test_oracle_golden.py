@@ -24,7 +24,7 @@ def run_oracle(case, precision="f32"):
     o.rho[:], o.u[:], o.flags[:], o.F[:] = f["rho"], f["u"], f["flags"], f["F"]
     o.initialize()
     o.run(case.steps, *case.force)
-    o.update_fields(*case.force)
+    case.settle_fields(o)
     if "ff" in case.extensions:
         o.update_force_field()
     return o

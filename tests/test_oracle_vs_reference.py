@@ -23,7 +23,8 @@ VARIANTS = [(19, "srt", "fp32", ("eq", "ff", "vf")), (19, "trt", "fp16s", ("eq",
             (27, "trt", "fp32", ("eq", "ff", "vf")), (27, "srt", "fp16s", ()),
             (19, "srt", "fp32", ("sg",)), (19, "trt", "fp16s", ("eq", "sg")), (27, "trt", "fp32", ("eq", "ff", "sg", "vf")),
             (19, "srt", "fp32", ("mb",)), (19, "trt", "fp16s", ("mb",)), (19, "trt", "fp16c", ("mb", "sg")),
-            (27, "trt", "fp32", ("eq", "ff", "mb", "vf"))]
+            (27, "trt", "fp32", ("eq", "ff", "mb", "vf")),
+            (19, "srt", "fp32", ("uf",)), (19, "trt", "fp16s", ("eq", "ff", "uf", "vf")), (27, "trt", "fp16c", ("eq", "mb", "uf"))]
 
 
 @pytest.mark.parametrize("variant", VARIANTS, ids=["_".join([str(v[0]), v[1], v[2], *v[3]]) for v in VARIANTS])
@@ -52,6 +53,9 @@ def test_random_flags_and_fields(variant):
         fx = 3e-5 if "vf" in ext else 0.0
         states.append(m.flags.copy())
         for steps in (1, 4):
+            if "uf" in ext:  # UPDATE_FIELDS: rho/u written by every step, compared before update_fields runs
+                m.run(1, fx, -1e-5 if fx else 0.0, 2e-5 if fx else 0.0)
+                states += [m.rho.copy(), m.u.copy()]
             if mb and steps == 4:  # some walls stop, the others change speed
                 solid = (m.flags & 3) == 1
                 m.u[:N][solid] *= np.float32(0.5)
