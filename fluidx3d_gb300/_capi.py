@@ -49,7 +49,8 @@ class AdjointConfig(ctypes.Structure):
 
 class AdjointStats(ctypes.Structure):
     _fields_ = [("forward_ms", ctypes.c_double), ("recompute_ms", ctypes.c_double), ("adjoint_ms", ctypes.c_double),
-                ("workspace_bytes", ctypes.c_uint64), ("levels", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+                ("workspace_bytes", ctypes.c_uint64), ("levels", ctypes.c_uint32), ("overlapped", ctypes.c_uint32),
+                ("reverse_ms", ctypes.c_double)]
 
 
 OBJECTIVES = {"ke_plane": 1, "drag_x": 2}

@@ -26,10 +26,13 @@ template<int Q> struct CellState {
 };
 
 // forward quantities of a fluid (or TYPE_E) cell
+// (1/rho from the hardware reciprocal and one Newton step: the adjoint is held to tolerances, not bits)
 template<int Q, bool VF> __device__ __forceinline__ void adj_forward(const float* g, const bool is_e, const float rho_p, const float* u_p, const float* Ft,
                                                                     CellState<Q>& s) {
+	float inv;
 	if(is_e) {
 		s.rho = rho_p;
+		inv = v_rcp(rho_p);
 		for(int d=0; d<3; d++) s.u0[d] = u_p[d];
 	} else {
 		float rho = g[0];
@@ -37,10 +40,10 @@ template<int Q, bool VF> __device__ __forceinline__ void adj_forward(const float
 		for(int i=1; i<Q; i++) rho += g[i];
 		rho += 1.0f;
 		s.rho = rho;
-		const float inv = 1.0f/rho;
+		inv = v_rcp(rho);
 		s.u0[0] = momentum<Q, 0>(g)*inv; s.u0[1] = momentum<Q, 1>(g)*inv; s.u0[2] = momentum<Q, 2>(g)*inv;
 	}
-	s.rho2 = 0.5f/s.rho;
+	s.rho2 = 0.5f*inv;
 	#pragma unroll
 	for(int d=0; d<3; d++) {
 		s.Ft[d] = Ft[d];
@@ -155,7 +158,7 @@ template<int Q, bool TRT, bool VF, class PUT> __device__ __forceinline__ void ad
 	}
 	float mbar[3] = {0.0f, 0.0f, 0.0f};
 	if(!is_e) {
-		const float inv = 1.0f/s.rho;
+		const float inv = 2.0f*s.rho2; // 1/rho
 		rhobar = fmaf(rho2bar, -2.0f*s.rho2*s.rho2, rhobar); // d(0.5/rho)/drho = -0.5/rho^2 = -2 rho2^2
 		#pragma unroll
 		for(int d=0; d<3; d++) { mbar[d] = u0bar[d]*inv; rhobar = fmaf(-u0bar[d]*inv, s.u0[d], rhobar); }
@@ -254,7 +257,10 @@ template<int Q, int ST, int EXT> __global__ void __launch_bounds__(256) k_object
 	const Grid& g = grid_of(a.g);
 	const uint64_t N = g.N;
 	double acc = 0.0;
-	for(uint64_t n=(uint64_t)blockIdx.x*256u+threadIdx.x; n<N; n+=(uint64_t)gridDim.x*256u) {
+	const bool plane = j.obj_kind==OBJ_KE_PLANE; // only the cells of plane x = plane_x, or every cell (drag)
+	const uint64_t M = plane ? (j.plane_x<g.Nx ? (uint64_t)g.Ny*g.Nz : 0ull) : N;
+	for(uint64_t k=(uint64_t)blockIdx.x*256u+threadIdx.x; k<M; k+=(uint64_t)gridDim.x*256u) {
+		const uint64_t n = plane ? (uint64_t)j.plane_x+k*g.Nx : k;
 		const uint8_t fl = a.flags[n];
 		const uint64_t z = n/g.NxNy;
 		const uint32_t xy = (uint32_t)(n-z*g.NxNy), y = xy/g.Nx, x = xy-y*g.Nx;

@@ -675,14 +675,14 @@ struct DeviceBuffer { // freed on scope exit
 // f^{k+1} = step(f^k) from src into dst: one thread per cell steps out of place (the row-staged
 // kernel when that path is forced); the two-cell kernels step in place only, so with one of those
 // forced the state is copied first
-int step_out_of_place(lbm_domain* d, const void* src, void* dst, const uint64_t t) {
+int step_out_of_place(lbm_domain* d, const void* src, void* dst, const uint64_t t, cudaStream_t stream) {
 	StepArgs a = d->args();
 	a.t = t;
 	a.fields_out = 0; // recomputed states leave the fields of the forward run alone
 	const bool rows_ok = row_plan(d->v.q, d->v.storage, d->g.Nx, d->g.Ny, d->g.Nz).stages!=0u;
 	int path = d->path==PATH_ROWS && rows_ok ? PATH_ROWS : PATH_CELLS;
 	if(d->path==PATH_PAIRS||d->path==PATH_PIPE) {
-		FX3D_CUDA(cudaMemcpyAsync(dst, src, d->field_bytes(LBM_FIELD_FI), cudaMemcpyDeviceToDevice, d->stream), "cudaMemcpyAsync(state)");
+		FX3D_CUDA(cudaMemcpyAsync(dst, src, d->field_bytes(LBM_FIELD_FI), cudaMemcpyDeviceToDevice, stream), "cudaMemcpyAsync(state)");
 		a.fi = dst; a.fi_dst = dst;
 		path = d->path;
 	} else {
@@ -690,12 +690,21 @@ int step_out_of_place(lbm_domain* d, const void* src, void* dst, const uint64_t 
 	}
 	cudaError_t e;
 	switch(d->v.storage) {
-		case ST_FP32: e = launch_stream_collide_fp32(d->v, a, path, d->stream); break;
-		case ST_FP16S: e = launch_stream_collide_fp16s(d->v, a, path, d->stream); break;
-		default: e = launch_stream_collide_fp16c(d->v, a, path, d->stream); break;
+		case ST_FP32: e = launch_stream_collide_fp32(d->v, a, path, stream); break;
+		case ST_FP16S: e = launch_stream_collide_fp16s(d->v, a, path, stream); break;
+		default: e = launch_stream_collide_fp16c(d->v, a, path, stream); break;
 	}
 	return e==cudaSuccess ? LBM_OK : cuda_fail(e, "stream_collide (recompute)");
 }
+
+struct StreamAndEvents { // a second stream and events for the overlapped reverse sweep, released on scope exit
+	cudaStream_t stream = nullptr;
+	cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+	~StreamAndEvents() {
+		if(stream) { cudaStreamSynchronize(stream); cudaStreamDestroy(stream); }
+		for(cudaEvent_t& e : ev) if(e) cudaEventDestroy(e);
+	}
+};
 
 struct EventTimer {
 	cudaEvent_t a = nullptr, b = nullptr;
@@ -743,7 +752,11 @@ extern "C" int lbm_run_adjoint(lbm_domain* d, const lbm_adjoint_config* cfg, dou
 	const size_t margin = 512ull<<20;
 	uint64_t K2 = K; // states kept per (sub-)segment
 	uint32_t levels = 1u;
-	size_t need = (nsnap+K)*SB+fixed;
+	// one level: a segment's states after its snapshot (K-1); with room for two such buffers the
+	// recomputation of the next segment runs on a second stream while the adjoint steps of this one run
+	size_t need = (nsnap+2ull*(K-1ull))*SB+fixed;
+	bool overlap = K>1ull && nsnap>1ull && need+margin<=free_b;
+	if(!overlap) need = (nsnap+K)*SB+fixed;
 	if(need+margin>free_b) {
 		levels = 2u;
 		K2 = 2ull; while(K2*K2<K) K2++; // >= 2: the recomputation ping-pongs between two states
@@ -753,7 +766,7 @@ extern "C" int lbm_run_adjoint(lbm_domain* d, const lbm_adjoint_config* cfg, dou
 	const uint64_t nsub = levels==2u ? (K+K2-1ull)/K2 : 0ull;
 	DeviceBuffer snaps, seg, sub, lam, grad, Jd;
 	FX3D_CUDA(cudaMalloc(&snaps.p, (size_t)nsnap*SB), "cudaMalloc(snapshots)");
-	FX3D_CUDA(cudaMalloc(&seg.p, (size_t)K2*SB), "cudaMalloc(segment states)");
+	FX3D_CUDA(cudaMalloc(&seg.p, (size_t)(overlap ? 2ull*(K-1ull) : K2)*SB), "cudaMalloc(segment states)");
 	if(levels==2u) FX3D_CUDA(cudaMalloc(&sub.p, (size_t)nsub*SB), "cudaMalloc(sub-snapshots)");
 	FX3D_CUDA(cudaMalloc(&lam.p, (size_t)d->cfg.velocity_set*N*4u), "cudaMalloc(adjoint DDFs)");
 	FX3D_CUDA(cudaMalloc(&grad.p, N*12u), "cudaMalloc(gradient)");
@@ -789,7 +802,7 @@ extern "C" int lbm_run_adjoint(lbm_domain* d, const lbm_adjoint_config* cfg, dou
 	auto reverse_states = [&](const uint64_t k0, const uint64_t k1, const void* start) -> int { // adjoint of steps k1-1 .. k0 from f^{k0} = start
 		EventTimer tr(d->stream);
 		FX3D_CUDA(cudaMemcpyAsync(segs(0), start, SB, cudaMemcpyDeviceToDevice, d->stream), "cudaMemcpyAsync(state)");
-		for(uint64_t k=k0; k+1ull<k1; k++) { const int r = step_out_of_place(d, segs(k-k0), segs(k-k0+1ull), t0+k); if(r!=LBM_OK) return r; }
+		for(uint64_t k=k0; k+1ull<k1; k++) { const int r = step_out_of_place(d, segs(k-k0), segs(k-k0+1ull), t0+k, d->stream); if(r!=LBM_OK) return r; }
 		recompute_ms += tr.stop(d->stream);
 		EventTimer ta(d->stream);
 		for(uint64_t k=k1; k-->k0;) {
@@ -799,7 +812,41 @@ extern "C" int lbm_run_adjoint(lbm_domain* d, const lbm_adjoint_config* cfg, dou
 		adjoint_ms += ta.stop(d->stream);
 		return LBM_OK;
 	};
-	for(uint64_t s=nsnap; s-->0ull;) {
+	EventTimer trev(d->stream);
+	StreamAndEvents ov;
+	if(overlap) {
+		// segment s uses buffer s%2 for its states k0+1 .. k1-1 (its first state is the snapshot itself).
+		// Stream R recomputes segment s-1 while the domain's stream runs the adjoint steps of segment s;
+		// R waits until the adjoint steps of segment s+1 have released the buffer it refills.
+		FX3D_CUDA(cudaStreamCreateWithFlags(&ov.stream, cudaStreamNonBlocking), "cudaStreamCreate");
+		for(cudaEvent_t& e : ov.ev) FX3D_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
+		cudaEvent_t* rec_done = ov.ev; cudaEvent_t* adj_done = ov.ev+2; cudaEvent_t start = ov.ev[4];
+		auto state = [&](const uint64_t sg, const uint64_t k) -> void* {
+			const uint64_t k0 = sg*K;
+			return k==k0 ? snap(sg) : (void*)((char*)seg.p+((size_t)(sg&1ull)*(K-1ull)+(size_t)(k-k0-1ull))*SB);
+		};
+		auto recompute = [&](const uint64_t sg, const bool wait_buffer) -> int {
+			const uint64_t k0 = sg*K, k1 = std::min<uint64_t>(k0+K, T);
+			if(wait_buffer) FX3D_CUDA(cudaStreamWaitEvent(ov.stream, adj_done[sg&1ull], 0), "cudaStreamWaitEvent");
+			for(uint64_t k=k0; k+1ull<k1; k++) { const int r = step_out_of_place(d, state(sg, k), state(sg, k+1ull), t0+k, ov.stream); if(r!=LBM_OK) return r; }
+			FX3D_CUDA(cudaEventRecord(rec_done[sg&1ull], ov.stream), "cudaEventRecord");
+			return LBM_OK;
+		};
+		FX3D_CUDA(cudaEventRecord(start, d->stream), "cudaEventRecord");
+		FX3D_CUDA(cudaStreamWaitEvent(ov.stream, start, 0), "cudaStreamWaitEvent"); // after lambda/grad are cleared
+		{ const int r = recompute(nsnap-1ull, false); if(r!=LBM_OK) return r; }
+		for(uint64_t sg=nsnap; sg-->0ull;) {
+			const uint64_t k0 = sg*K, k1 = std::min<uint64_t>(k0+K, T);
+			if(sg>=1ull) { const int r = recompute(sg-1ull, sg+1ull<nsnap); if(r!=LBM_OK) return r; }
+			FX3D_CUDA(cudaStreamWaitEvent(d->stream, rec_done[sg&1ull], 0), "cudaStreamWaitEvent");
+			for(uint64_t k=k1; k-->k0;) {
+				j.state = state(sg, k); j.obj_weight = in_window(t0+k) ? (float)weight : 0.0f;
+				FX3D_CUDA(launch_adjoint_step(d->v, args_at(t0+k, j.state), j, false, d->stream), "adjoint step");
+			}
+			FX3D_CUDA(cudaEventRecord(adj_done[sg&1ull], d->stream), "cudaEventRecord");
+		}
+	}
+	for(uint64_t s=nsnap; !overlap && s-->0ull;) {
 		const uint64_t k0 = s*K, k1 = std::min<uint64_t>(k0+K, T);
 		if(levels==1u) { const int r = reverse_states(k0, k1, snap(s)); if(r!=LBM_OK) return r; continue; }
 		// two levels: sub-snapshots every K2 steps of the segment, then each sub-segment in reverse
@@ -808,7 +855,7 @@ extern "C" int lbm_run_adjoint(lbm_domain* d, const lbm_adjoint_config* cfg, dou
 		FX3D_CUDA(cudaMemcpyAsync(segs(0), snap(s), SB, cudaMemcpyDeviceToDevice, d->stream), "cudaMemcpyAsync(state)");
 		for(uint64_t k=k0; k+1ull<k1; k++) {
 			void* a0 = segs((k-k0)%2ull); void* a1 = segs((k-k0+1ull)%2ull);
-			const int r = step_out_of_place(d, a0, a1, t0+k); if(r!=LBM_OK) return r;
+			const int r = step_out_of_place(d, a0, a1, t0+k, d->stream); if(r!=LBM_OK) return r;
 			if((k+1ull-k0)%K2==0ull) FX3D_CUDA(cudaMemcpyAsync(subs((k+1ull-k0)/K2), a1, SB, cudaMemcpyDeviceToDevice, d->stream), "cudaMemcpyAsync(sub-snapshot)");
 		}
 		recompute_ms += tr.stop(d->stream);
@@ -817,6 +864,7 @@ extern "C" int lbm_run_adjoint(lbm_domain* d, const lbm_adjoint_config* cfg, dou
 			if(r!=LBM_OK) return r;
 		}
 	}
+	const double reverse_ms = trev.stop(d->stream);
 	double Jh = 0.0;
 	FX3D_CUDA(cudaMemcpyAsync(&Jh, Jd.p, sizeof(double), cudaMemcpyDeviceToHost, d->stream), "cudaMemcpyAsync(J)");
 	if(gradient) FX3D_CUDA(cudaMemcpyAsync(gradient, grad.p, N*12u, cudaMemcpyDeviceToHost, d->stream), "cudaMemcpyAsync(gradient)");
@@ -825,7 +873,8 @@ extern "C" int lbm_run_adjoint(lbm_domain* d, const lbm_adjoint_config* cfg, dou
 	if(objective) *objective = Jh;
 	if(stats) {
 		stats->forward_ms = forward_ms; stats->recompute_ms = recompute_ms; stats->adjoint_ms = adjoint_ms;
-		stats->workspace_bytes = (uint64_t)need; stats->levels = levels; stats->reserved = 0u;
+		stats->workspace_bytes = (uint64_t)need; stats->levels = levels; stats->overlapped = overlap ? 1u : 0u;
+		stats->reverse_ms = reverse_ms;
 	}
 	d->t_last_update_fields = d->fused_fields ? d->t : UINT64_MAX;
 	d->t_last_force_field = UINT64_MAX;

@@ -330,6 +330,73 @@ template<int Q, int ST, typename T> __device__ __forceinline__ void issue_pair(c
 	});
 }
 
+// Byte offsets of both cells of a pair (x even, x+1) and of their neighbours at one z plane, for
+// lattices whose DDF arrays are under 4 GB each (N * sizeof(T) < 2^32). Steps carry the periodic wrap
+// as Steps32 does, in bytes; what differs from two Steps32 is what the pair's geometry fixes: with
+// Nx and x even, cell x+1 never wraps towards -x and cell x never towards +x, and both share their y
+// and z steps. Each access is a 64-bit uniform array base plus a 32-bit per-thread offset.
+template<int E> struct PairSteps {
+	uint32_t n, xm_a, xp_b, yp, ym, zp, zm;
+	__device__ __forceinline__ PairSteps(const Grid& g, const uint32_t x, const uint32_t y, const uint32_t z, const uint32_t n_) {
+		const uint32_t N = (uint32_t)g.N;
+		n = n_*(uint32_t)E;
+		xm_a = (x==0u ? g.Nx-1u : 0xFFFFFFFFu)*(uint32_t)E;
+		xp_b = (x+2u==g.Nx ? 1u-g.Nx : 1u)*(uint32_t)E;
+		yp = (y+1u==g.Ny ? g.Nx-g.NxNy : g.Nx)*(uint32_t)E;
+		ym = (y==0u ? g.NxNy-g.Nx : 0u-g.Nx)*(uint32_t)E;
+		zp = (z+1u==g.Nz ? g.NxNy-N : g.NxNy)*(uint32_t)E;
+		zm = (z==0u ? N-g.NxNy : 0u-g.NxNy)*(uint32_t)E;
+	}
+	template<int I> __device__ __forceinline__ uint32_t yz() const {
+		constexpr int b = vs_c(1, I), c = vs_c(2, I);
+		const uint32_t sy = b>0 ? yp : b<0 ? ym : 0u, sz = c>0 ? zp : c<0 ? zm : 0u;
+		return b!=0 && c!=0 ? sy+sz : b!=0 ? sy : c!=0 ? sz : 0u;
+	}
+	template<int I> __device__ __forceinline__ uint32_t ja() const { // neighbour of cell x along c_I
+		constexpr int a = vs_c(0, I);
+		return a>0 ? n+(uint32_t)E+yz<I>() : a<0 ? n+xm_a+yz<I>() : n+yz<I>();
+	}
+	template<int I> __device__ __forceinline__ uint32_t jb() const { // neighbour of cell x+1 along c_I
+		constexpr int a = vs_c(0, I);
+		return a>0 ? n+(uint32_t)E+xp_b+yz<I>() : a<0 ? n+yz<I>() : n+(uint32_t)E+yz<I>();
+	}
+};
+template<typename T> __device__ __forceinline__ const T* at(const T* base, const uint32_t off) { return (const T*)((const char*)base+off); }
+template<typename T> __device__ __forceinline__ T* at(T* base, const uint32_t off) { return (T*)((char*)base+off); }
+
+template<int Q, int ST, typename T> __device__ __forceinline__ void issue_pair_b(const T* __restrict__ fi, const uint8_t* __restrict__ flags, const uint64_t N,
+                                                                                 const PairSteps<sizeof(T)>& p, const uint32_t nc, const bool odd, const uint32_t s0) {
+	constexpr uint32_t W = 2u*sizeof(T), STRIDE = BLOCK*W;
+	auto cpw = [](const uint32_t d, const T* q) { if constexpr(W==4u) cp_async_4(d, q); else cp_async_8(d, q); };
+	const uint64_t e = odd ? 0ull : N;
+	cp_async_4(s0, flags+(nc&~3u));
+	cpw(s0+STRIDE, at(fi, p.n));
+	Unroll<1, Q, 2>::run([&](auto ic) {
+		constexpr int i = decltype(ic)::value;
+		constexpr uint32_t ka = 2u+(uint32_t)(i-1)/2u, kb = (uint32_t)pair_b_item<Q>(i);
+		const T* pa = fi+((uint64_t)i*N+e);
+		const T* pb = fi+((uint64_t)(i+1)*N-e);
+		cpw(s0+ka*STRIDE, at(pa, p.n));
+		if constexpr(vs_c(0, i)==0) cpw(s0+kb*STRIDE, at(pb, p.template ja<i>()));
+		else if constexpr(W==4u) { cp_async_4(s0+kb*STRIDE, at(pb, p.template ja<i>()-(uint32_t)sizeof(T))); cp_async_4(s0+(kb+1u)*STRIDE, at(pb, p.template jb<i>())); }
+		else { cp_async_4(s0+kb*STRIDE, at(pb, p.template ja<i>())); cp_async_4(s0+(kb+1u)*STRIDE, at(pb, p.template jb<i>())); }
+	});
+}
+template<int Q, int ST, typename T> __device__ __forceinline__ void store_pair_b(T* __restrict__ fi, const uint64_t N, const PairSteps<sizeof(T)>& p,
+                                                                                 const bool odd, const float2* f) {
+	typedef RawCodec<ST> CD;
+	const uint64_t e = odd ? 0ull : N;
+	PairIO<ST>::store2(at(fi, p.n), f[0]);
+	Unroll<1, Q, 2>::run([&](auto ic) {
+		constexpr int i = decltype(ic)::value;
+		T* pa = fi+((uint64_t)i*N+e);
+		T* pb = fi+((uint64_t)(i+1)*N-e);
+		if constexpr(vs_c(0, i)==0) PairIO<ST>::store2(at(pb, p.template ja<i>()), f[i]);
+		else { *at(pb, p.template ja<i>()) = CD::encode(f[i].x); *at(pb, p.template jb<i>()) = CD::encode(f[i].y); }
+		PairIO<ST>::store2(at(pa, p.n), f[i+1]);
+	});
+}
+
 // the pair's values from its staged items (item k of this thread at w[k*BLOCK])
 template<int ST> struct PairStage;
 template<> struct PairStage<ST_FP32> {
@@ -367,6 +434,9 @@ template<int Q, int ST> __device__ __forceinline__ void read_pair(const typename
 #ifndef FX3D_PIPE_MIN_BLOCKS
 #define FX3D_PIPE_MIN_BLOCKS 3
 #endif
+#ifndef FX3D_PIPE_BYTE_OFFSETS
+#define FX3D_PIPE_BYTE_OFFSETS 0
+#endif
 #ifndef FX3D_PIPE_REREAD
 #define FX3D_PIPE_REREAD 0
 #endif
@@ -396,8 +466,12 @@ template<int Q, int ST, bool TRT, int EXT, int S> __global__ void __launch_bound
 	const uint32_t s0 = smem_u32(w0);
 	auto issue = [&](const uint32_t z, const int stage) {
 		const uint32_t n = z*g.NxNy+xy;
+#if FX3D_PIPE_BYTE_OFFSETS
+		issue_pair_b<Q, ST>((const T*)a.fi, a.flags, g.N, PairSteps<sizeof(T)>(g, x, y, z, n), n, odd, s0+(uint32_t)(stage*ITEMS*BLOCK)*(uint32_t)sizeof(SW));
+#else
 		const Steps32 sa(g, x, y, z, n), sb(g, x+1u, y, z, n+1u);
 		issue_pair<Q, ST>((const T*)a.fi, a.flags, g.N, sa, sb, odd, s0+(uint32_t)(stage*ITEMS*BLOCK)*(uint32_t)sizeof(SW));
+#endif
 	};
 	#pragma unroll
 	for(int s=0; s<S-1; s++) {
@@ -448,7 +522,9 @@ template<int Q, int ST, bool TRT, int EXT, int S> __global__ void __launch_bound
 			store_f32<Q, RawCodec<ST>>((T*)a.fi, g.N, s, odd, f1);
 			continue;
 		}
+#if !FX3D_PIPE_BYTE_OFFSETS
 		const Steps32 sa(g, x, y, z, n), sb(g, x+1u, y, z, n+1u);
+#endif
 		const Bool2 is_e{EQ && (fa&TYPE_BO)==TYPE_E, EQ && (fb&TYPE_BO)==TYPE_E};
 		const bool any_e = is_e.x||is_e.y;
 		float2 R, Rm1, inv, ux, uy, uz, fx, fy, fz;
@@ -460,7 +536,11 @@ template<int Q, int ST, bool TRT, int EXT, int S> __global__ void __launch_bound
 		}
 		if(any_e) collide_v<Q, TRT, VF, ST, 2, float2, Bool2, (EXT&EXT_SG)!=0>(f, R, Rm1, ux, uy, uz, fx, fy, fz, is_e, a);
 		else collide_v<Q, TRT, VF, ST, 0, float2, Bool2, (EXT&EXT_SG)!=0>(f, R, Rm1, ux, uy, uz, fx, fy, fz, is_e, a);
+#if FX3D_PIPE_BYTE_OFFSETS
+		store_pair_b<Q, ST>((T*)a.fi, g.N, PairSteps<sizeof(T)>(g, x, y, z, n), odd, f);
+#else
 		store_pair<Q, ST>((T*)a.fi, g.N, sa, sb, odd, f);
+#endif
 	}
 }
 

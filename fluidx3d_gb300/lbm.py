@@ -234,7 +234,7 @@ class LBM:
         grad = np.empty(3 * self.get_N(), np.float32)
         st = C.AdjointStats()
         self._check(C.load().lbm_run_adjoint(self._d, ctypes.byref(cfg), ctypes.byref(J), grad.ctypes.data, ctypes.byref(st)))
-        stats = {k: getattr(st, k) for k, _ in C.AdjointStats._fields_ if k != "reserved"}
+        stats = {k: getattr(st, k) for k, _ in C.AdjointStats._fields_}
         return J.value, grad, stats
 
     # ------------------------------------------------------------------ geometry (src/lbm.cpp:1074-1093)

@@ -184,10 +184,13 @@ typedef struct lbm_adjoint_config {
 	uint64_t window_begin, window_end; /* J is the mean over the states after these time steps (inclusive) */
 } lbm_adjoint_config;
 typedef struct lbm_adjoint_stats {
-	double forward_ms, recompute_ms, adjoint_ms; /* device time of the three phases */
-	uint64_t workspace_bytes;                    /* snapshots + recomputed states + adjoint DDFs + gradient */
-	uint32_t levels;                             /* 1: every state of a segment kept; 2: sub-snapshots inside segments */
-	uint32_t reserved;
+	double forward_ms;            /* device time of the forward sweep (steps, snapshots, objective) */
+	double recompute_ms, adjoint_ms; /* device time of the recomputation and of the adjoint steps when they run one
+	                               * after the other; 0 when they overlap (overlapped = 1): then see reverse_ms */
+	uint64_t workspace_bytes;     /* snapshots + recomputed states + adjoint DDFs + gradient */
+	uint32_t levels;              /* 1: every state of a segment kept; 2: sub-snapshots inside segments */
+	uint32_t overlapped;          /* 1: the next segment was recomputed on a second stream during the adjoint steps */
+	double reverse_ms;            /* device time of the whole reverse sweep (recomputation and adjoint steps) */
 } lbm_adjoint_stats;
 /* J (objective, may be NULL), dJ/dF (gradient: host float[3N] SoA, may be NULL), stats (may be NULL) */
 int lbm_run_adjoint(lbm_domain* domain, const lbm_adjoint_config* config, double* objective, float* gradient, lbm_adjoint_stats* stats);

@@ -87,3 +87,26 @@ def test_errors_are_reported_not_fatal(gpu):
         assert b"bytes" in C.load().lbm_last_error() or b"field" in C.load().lbm_last_error()
         lbm.run(3)  # the domain stays usable
         assert lbm.get_t() == 3
+
+
+@pytest.mark.parametrize("arithmetic,path", [("exact", "cells"), ("fast", "cells"), ("fast", "pipe"), ("fast", "pairs")])
+def test_fused_update_fields_lag_one_step(arithmetic, path, gpu, monkeypatch):
+    """UPDATE_FIELDS: after run(k) rho/u are the fields of the state at t = k-1, bit for bit what
+    update_fields gives after run(k-1) without the extension (TYPE_E cells keep their preset values);
+    update_fields is a no-op; the reference's byte accounting adds 16 B per cell."""
+    monkeypatch.setenv("FX3D_STREAM_COLLIDE_PATH", path)
+    base = LC.CASE_BY_NAME["d3q19_trt_fp16s_channel_eq_ff_vf"]
+    fused_case = LC.Case("fused", base.q, base.collision, base.storage, base.extensions + ("uf",), base.geometry, fx=base.fx)
+    with make_gpu(base, arithmetic) as plain, make_gpu(fused_case, arithmetic) as fused:
+        plain.run(6)
+        plain.update_fields()
+        fused.run(7)
+        for lbm in (plain, fused):
+            lbm.rho.read_from_device()
+            lbm.u.read_from_device()
+        assert np.array_equal(fused.rho.data, plain.rho.data)
+        assert np.array_equal(fused.u.data, plain.u.data)
+        fused.update_fields()
+        fused.u.read_from_device()
+        assert np.array_equal(fused.u.data, plain.u.data)
+        assert fused.bandwidth_bytes_per_cell() == plain.bandwidth_bytes_per_cell() + 16
