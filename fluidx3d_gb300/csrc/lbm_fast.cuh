@@ -128,23 +128,28 @@ template<int C, class V> __device__ __forceinline__ void acc_signed(V& m, bool& 
 }
 
 // S = K*(rho-1) = sum of the shifted DDFs and the momentum (storage units), from pair sums and pair
-// differences; the shift K is added only afterwards (R = S+K), so S keeps full precision
-template<int Q, class V> __device__ __forceinline__ void moments_v(const V* f, V& S, V& mx, V& my, V& mz) {
+// differences; the shift K is added only afterwards (R = S+K), so S keeps full precision. The pair
+// sums and differences replace the pair's DDFs in f (f[i] = f_i + f_j, f[i+1] = f_i - f_j for the
+// opposite pair (i, j = i+1)): the collision works on them directly.
+template<int Q, class V> __device__ __forceinline__ void moments_v(V* f, V& S, V& mx, V& my, V& mz) {
 	V s = f[0];
 	bool sx = false, sy = false, sz = false;
 	mx = v_set<V>(0.0f); my = v_set<V>(0.0f); mz = v_set<V>(0.0f);
 	Unroll<1, Q, 2>::run([&](auto ic) {
 		constexpr int i = decltype(ic)::value;
-		s = v_add(s, v_add(f[i], f[i+1]));
-		const V d = v_sub(f[i], f[i+1]);
+		const V p = v_add(f[i], f[i+1]), d = v_sub(f[i], f[i+1]);
+		s = v_add(s, p);
 		acc_signed<vs_c(0, i)>(mx, sx, d); acc_signed<vs_c(1, i)>(my, sy, d); acc_signed<vs_c(2, i)>(mz, sz, d);
+		f[i] = p; f[i+1] = d;
 	});
 	S = s;
 }
 
 // velocity of the cell(s) (storage-unit DDFs, or the preset rho/u of TYPE_E cells), force shifted and
 // clamped; R = K*rho, Rm1 = K*(rho-1), inv = 1/R. is_e: per-lane TYPE_E flags, any_e: any of them.
-template<int Q, int EXT, int ST, class V, class M> __device__ __forceinline__ void cell_rho_u_v(const StepArgs& a, const uint64_t n, const V* f, const M is_e,
+// The opposite pairs of f leave in pair-sum / pair-difference form (moments_v), except for a single
+// TYPE_E cell (float), whose collision does not read f.
+template<int Q, int EXT, int ST, class V, class M> __device__ __forceinline__ void cell_rho_u_v(const StepArgs& a, const uint64_t n, V* f, const M is_e,
                                                                                             const bool any_e, V& R, V& Rm1, V& inv, V& ux, V& uy, V& uz,
                                                                                             V& fx, V& fy, V& fz) {
 	constexpr bool VF = (EXT&EXT_VF)!=0, FF = (EXT&EXT_FF)!=0;
@@ -194,22 +199,29 @@ template<int Q, int EXT, int ST, class V, class M> __device__ __forceinline__ vo
 
 // collision rates as values of V: uniform (the host's rates) or per cell (SUBGRID)
 template<class V> struct VRates {
-	V w, hp, hm, nhm, half_c_tau, c_taup, c_taum;
+	V cs, cb, cd, cu, fp, fm; // 1/2 - hp, 2 hp, 1/2 - hm, 2 hm, Guo factors of G_i + G_j and G_i - G_j
 	V rest_rate, rest_force; // the rest direction's relaxation and Guo factors (SRT: w, c_tau; TRT: 2 hp, 2 c_taup)
 };
-struct LaneRates { float w, hp, hm, nhm, half_c_tau, c_taup, c_taum, rest_rate, rest_force; };
+// Rates of the pair-sum / pair-difference form of the collision. With S = f_i + f_j, D = f_i - f_j
+// for an opposite pair, feq_{i,j} = base +- rw uk and d = feq - f, the TRT update
+// f_i += hp (d_i + d_j) + hm (d_i - d_j) is, with f_i = (S + D)/2,
+//   f_i' = P + M, f_j' = P - M,  P = (1/2 - hp) S + 2 hp base,  M = (1/2 - hm) D + 2 hm rw uk,
+// and SRT is the case hp = hm = w/2. The Guo terms add c+ (G_i + G_j) to P and c- (G_i - G_j) to M
+// (SRT: c+ = c- = c_tau/2).
+struct LaneRates { float cs, cb, cd, cu, fp, fm, rest_rate, rest_force; };
 template<bool TRT> __device__ __forceinline__ LaneRates lane_rates(const float w, const float hp, const float hm, const float c_tau, const float c_taup,
                                                                  const float c_taum) {
-	return LaneRates{w, hp, hm, -hm, 0.5f*c_tau, c_taup, c_taum, !TRT ? w : 2.0f*hp, !TRT ? c_tau : 2.0f*c_taup};
+	const float hm_ = TRT ? hm : hp; // hp = w/2
+	return LaneRates{__fsub_rn(0.5f, hp), __fadd_rn(hp, hp), __fsub_rn(0.5f, hm_), __fadd_rn(hm_, hm_), TRT ? c_taup : 0.5f*c_tau, TRT ? c_taum : 0.5f*c_tau,
+	                 !TRT ? w : 2.0f*hp, !TRT ? c_tau : 2.0f*c_taup};
 }
 template<class V> __device__ __forceinline__ VRates<V> v_rates(const LaneRates& a);
 template<> __device__ __forceinline__ VRates<float> v_rates<float>(const LaneRates& a) {
-	return VRates<float>{a.w, a.hp, a.hm, a.nhm, a.half_c_tau, a.c_taup, a.c_taum, a.rest_rate, a.rest_force};
+	return VRates<float>{a.cs, a.cb, a.cd, a.cu, a.fp, a.fm, a.rest_rate, a.rest_force};
 }
 __device__ __forceinline__ VRates<float2> v_rates2(const LaneRates& a, const LaneRates& b) {
-	return VRates<float2>{make_float2(a.w, b.w), make_float2(a.hp, b.hp), make_float2(a.hm, b.hm), make_float2(a.nhm, b.nhm),
-	                      make_float2(a.half_c_tau, b.half_c_tau), make_float2(a.c_taup, b.c_taup), make_float2(a.c_taum, b.c_taum),
-	                      make_float2(a.rest_rate, b.rest_rate), make_float2(a.rest_force, b.rest_force)};
+	return VRates<float2>{make_float2(a.cs, b.cs), make_float2(a.cb, b.cb), make_float2(a.cd, b.cd), make_float2(a.cu, b.cu),
+	                      make_float2(a.fp, b.fp), make_float2(a.fm, b.fm), make_float2(a.rest_rate, b.rest_rate), make_float2(a.rest_force, b.rest_force)};
 }
 template<> __device__ __forceinline__ VRates<float2> v_rates<float2>(const LaneRates& a) { return v_rates2(a, a); }
 // SUBGRID rates of one cell from its stress tensor H (storage units) and 1/R, with the hardware
@@ -238,12 +250,13 @@ template<int I, class V> __device__ __forceinline__ void stress_add_v(V* H, cons
 	if constexpr(cy!=0 && cz!=0) H[5] = cy*cz>0 ? v_add(H[5], s) : v_sub(H[5], s);
 }
 
-// collision of all directions in place, DDFs in storage units (K scaling). EMODE 0: no TYPE_E cell;
-// 1: the (single) cell is TYPE_E (f = feq); 2: mixed lanes, TYPE_E lanes picked by is_e. SG: the
-// relaxation rate of each cell from the Smagorinsky-Lilly model (src/kernel.cpp:1579-1593); the
-// stress tensor comes from pair sums f_i + f_j - (feq_i + feq_j), feq_i + feq_j = 2 base, and the
-// rate itself from the same scalar operations in either form of V (sqrt(H:H)/rho is the same in
-// storage units, H and R both carry the factor K).
+// collision of all directions in place, DDFs in storage units (K scaling), the opposite pairs of f
+// in pair-sum / pair-difference form on entry (moments_v) and as DDFs on exit. EMODE 0: no TYPE_E
+// cell; 1: the (single) cell is TYPE_E (f = feq, f not read); 2: mixed lanes, TYPE_E lanes picked by
+// is_e. SG: the relaxation rate of each cell from the Smagorinsky-Lilly model
+// (src/kernel.cpp:1579-1593); the stress tensor comes from the pair sums S - (feq_i + feq_j),
+// feq_i + feq_j = 2 base, and the rate itself from the same scalar operations in either form of V
+// (sqrt(H:H)/rho is the same in storage units, H and R both carry the factor K).
 template<int Q, bool TRT, bool VF, int ST, int EMODE, class V, class M, bool SG = false> __device__ __forceinline__ void collide_v(V* f, const V R, const V Rm1,
                                                                                                              const V ux, const V uy, const V uz,
                                                                                                              const V fx, const V fy, const V fz,
@@ -256,13 +269,13 @@ template<int Q, bool TRT, bool VF, int ST, int EMODE, class V, class M, bool SG 
 		fxK = v_mul(v_set<V>(K), fx); fyK = v_mul(v_set<V>(K), fy); fzK = v_mul(v_set<V>(K), fz);
 		uF = v_mul(v_set<V>(-THIRD), v_fma(ux, fxK, v_fma(uy, fyK, v_mul(uz, fzK))));
 	}
-	// w R, w R / 2 and w (R-K) once per weight class (straight, edge, corner directions)
+	// w R / 2 and w (R-K) once per weight class (straight, edge, corner directions): base = w R/2 (uk^2 + c3) + w (R-K)
 	constexpr int NC = Q==27 ? 3 : 2;
-	V rwc[NC], nrwc[NC], hrc[NC], wmc[NC];
+	V hrc[NC], wmc[NC];
 	#pragma unroll
 	for(int c=0; c<NC; c++) {
 		const float wc = vs_w<Q>(c==0 ? 1 : c==1 ? 7 : 19);
-		rwc[c] = v_mul(v_set<V>(wc), R); nrwc[c] = v_mul(v_set<V>(-wc), R); hrc[c] = v_mul(v_set<V>(0.5f*wc), R); wmc[c] = v_mul(v_set<V>(wc), Rm1);
+		hrc[c] = v_mul(v_set<V>(0.5f*wc), R); wmc[c] = v_mul(v_set<V>(wc), Rm1);
 	}
 	auto base_of = [&](auto ic, V& uk) { // the shared equilibrium term of pair (i, i+1)
 		constexpr int i = decltype(ic)::value;
@@ -279,7 +292,7 @@ template<int Q, bool TRT, bool VF, int ST, int EMODE, class V, class M, bool SG 
 			constexpr int i = decltype(ic)::value;
 			V uk;
 			const V base = base_of(ic, uk);
-			stress_add_v<i>(H, v_sub(v_add(f[i], f[i+1]), v_add(base, base)));
+			stress_add_v<i>(H, v_sub(f[i], v_add(base, base)));
 		});
 		const float tau0 = __fdiv_rn(1.0f, a.w); // uniform
 		const V inv = v_rcp(R);
@@ -302,43 +315,42 @@ template<int Q, bool TRT, bool VF, int ST, int EMODE, class V, class M, bool SG 
 			if constexpr(EMODE==2) f[0] = v_pick(g0, v_mul(w0, X), is_e); else f[0] = g0;
 		}
 	}
+	// 2 hm w R per weight class (the factor of uk in M)
+	V cuc[NC];
+	if constexpr(EMODE!=1) {
+		const V cuR = v_mul(r.cu, R);
+		#pragma unroll
+		for(int c=0; c<NC; c++) cuc[c] = v_mul(v_set<V>(vs_w<Q>(c==0 ? 1 : c==1 ? 7 : 19)), cuR);
+	}
 	Unroll<1, Q, 2>::run([&](auto ic) {
 		constexpr int i = decltype(ic)::value;
 		constexpr int c = (vs_c(0, i)!=0)+(vs_c(1, i)!=0)+(vs_c(2, i)!=0)-1;
 		const float wi = vs_w<Q>(i);
 		V uk;
 		const V base = base_of(ic, uk);
-		const V ea = v_fma(rwc[c], uk, base), eb = v_fma(nrwc[c], uk, base);
-		if constexpr(EMODE==1) { f[i] = ea; f[i+1] = eb; }
-		else {
-			const V da = v_sub(ea, f[i]), db = v_sub(eb, f[i+1]);
-			V na, nb;
-			if constexpr(!TRT) { na = v_fma(r.w, da, f[i]); nb = v_fma(r.w, db, f[i+1]); }
-			else {
-				const V t = v_mul(r.hp, v_add(da, db)), dd = v_sub(da, db);
-				na = v_add(f[i], v_fma(r.hm, dd, t)); nb = v_add(f[i+1], v_fma(r.nhm, dd, t));
-			}
+		if constexpr(EMODE==1) { // f = feq = base +- w R uk
+			const V rw = v_mul(v_set<V>(wi), R);
+			f[i] = v_fma(rw, uk, base); f[i+1] = v_fma(v_neg(rw), uk, base);
+		} else {
+			V P = v_fma(r.cs, f[i], v_mul(r.cb, base));
+			V Mn = v_fma(r.cd, f[i+1], v_mul(cuc[c], uk));
 			if constexpr(VF) {
 				const V cf = csum_v<i>(fxK, fyK, fzK);
 				const V Y = v_fma(cf, v_mul(uk, v_set<V>(THIRD)), uF);
-				const V gd = v_mul(v_set<V>(6.0f*wi), cf);                     // G_i - G_j
-				if constexpr(!TRT) { // G_i = gs + gd and G_j = gs - gd, each one fused operation
-					na = v_fma(r.half_c_tau, v_fma(v_set<V>(18.0f*wi), Y, gd), na);
-					nb = v_fma(r.half_c_tau, v_fma(v_set<V>(18.0f*wi), Y, v_neg(gd)), nb);
-				} else {
-					const V gs = v_mul(v_set<V>(18.0f*wi), Y);                 // G_i + G_j  (c.u = uk/3)
-					const V m = v_mul(r.c_taum, gd);
-					na = v_add(na, v_fma(r.c_taup, gs, m)); nb = v_add(nb, v_fma(r.c_taup, gs, v_neg(m)));
-				}
+				P = v_fma(r.fp, v_mul(v_set<V>(18.0f*wi), Y), P);          // G_i + G_j = 18 w Y  (c.u = uk/3)
+				Mn = v_fma(r.fm, v_mul(v_set<V>(6.0f*wi), cf), Mn);         // G_i - G_j = 6 w (c.F)
 			}
-			if constexpr(EMODE==2) { f[i] = v_pick(na, ea, is_e); f[i+1] = v_pick(nb, eb, is_e); }
-			else { f[i] = na; f[i+1] = nb; }
+			const V na = v_add(P, Mn), nb = v_sub(P, Mn);
+			if constexpr(EMODE==2) {
+				const V rw = v_mul(v_set<V>(wi), R);
+				f[i] = v_pick(na, v_fma(rw, uk, base), is_e); f[i+1] = v_pick(nb, v_fma(v_neg(rw), uk, base), is_e);
+			} else { f[i] = na; f[i+1] = nb; }
 		}
 	});
 }
 
 // ---------------------------------------------------------------- one cell (the scalar kernels)
-template<int Q, int EXT, int ST> __device__ __forceinline__ void cell_rho_u_fast(const StepArgs& a, const uint64_t n, const float* f, const bool is_e,
+template<int Q, int EXT, int ST> __device__ __forceinline__ void cell_rho_u_fast(const StepArgs& a, const uint64_t n, float* f, const bool is_e,
                                                                                 float& R, float& Rm1, float& inv, float& ux, float& uy, float& uz,
                                                                                 float& fx, float& fy, float& fz) {
 	cell_rho_u_v<Q, EXT, ST, float>(a, n, f, is_e, is_e, R, Rm1, inv, ux, uy, uz, fx, fy, fz);

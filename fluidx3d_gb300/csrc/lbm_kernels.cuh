@@ -253,6 +253,10 @@ template<int ST> __device__ __forceinline__ void store_pair_fields(const StepArg
 
 inline dim3 pair_grid(const GridDesc& g) { return dim3((g.NxNy/2u+BLOCK-1u)/BLOCK, g.Nz, 1u); }
 inline bool pairs_supported(const GridDesc& g) { return g.Nx%2u==0u && g.N<=0xFFFFFFFFull; }
+#ifndef FX3D_PIPE_BLOCK
+#define FX3D_PIPE_BLOCK 256
+#endif
+constexpr int PIPE_BLOCK = FX3D_PIPE_BLOCK; // threads per block of the prefetching two-cell kernel
 
 #ifndef FX3D_PAIRS_MIN_BLOCKS
 #define FX3D_PAIRS_MIN_BLOCKS 2 // resident 256-thread blocks per SM the register budget is sized for
@@ -295,14 +299,18 @@ template<int Q, int ST, bool TRT, int EXT> __global__ void __launch_bounds__(BLO
 // Two-cell kernel with per-thread prefetch. A thread walks the pairs (x0, y, z) of a column of z
 // planes; while it steps one pair, the DDF words of the next S-1 pairs are already in flight as
 // per-thread cp.async copies into its own shared-memory slots (item k of stage s at
-// smem[(s*ITEMS + k)*BLOCK + thread]), so every warp keeps loads outstanding through its compute and
+// smem[(s*ITEMS + k)*PIPE_BLOCK + thread]), so every warp keeps loads outstanding through its compute and
 // store phases without holding them in registers, and no block-wide barrier is needed. Per pair the
 // items are: the aligned 4-byte flags word holding both cells' flags, the rest slot, the own slots
 // of each direction pair, and for each neighbour slot either one aligned pair word (c_x = 0) or two
 // words (c_x != 0): for FP16 the aligned words holding the first cell's value in their upper half
 // (index j-1, j odd) and the second cell's value in their lower half (j even), for FP32 the two
 // values themselves. Values next to them belong to other cells and are read but never used.
-// Results are bit-identical to the plain two-cell kernel: only where the loads land differs.
+// Slot addresses are per-thread indices onto the launch's slot table (SlotTable). Results are
+// bit-identical to the plain two-cell kernel: only where the loads land differs.
+// Walk length and block size (measured on 512x256x256 D3Q19 TRT FP16S, GB300): 2 z planes per
+// thread in 256-thread blocks, 0.545 ms per step; 4 planes 0.567 ms (128-thread blocks), 8 planes
+// 0.586 ms. Shorter walks lose the prefetch of the first pair but even out the blocks' run times.
 template<int Q> __host__ __device__ constexpr int pair_nx0() { int c = 0; for(int i=1; i<Q; i+=2) if(vs_c(0, i)==0) c++; return c; }
 template<int Q> __host__ __device__ constexpr int pair_items() { return 2+(Q-1)/2+pair_nx0<Q>()+2*((Q-1)/2-pair_nx0<Q>()); }
 template<int Q> __host__ __device__ constexpr int pair_b_item(const int i) { // first item of the neighbour slot of pair (i, i+1)
@@ -311,112 +319,71 @@ template<int Q> __host__ __device__ constexpr int pair_b_item(const int i) { // 
 	return k;
 }
 
-template<int Q, int ST, typename T> __device__ __forceinline__ void issue_pair(const T* __restrict__ fi, const uint8_t* __restrict__ flags, const uint64_t N,
-                                                                               const Steps32& sa, const Steps32& sb, const bool odd, const uint32_t s0) {
-	constexpr uint32_t W = 2u*sizeof(T), STRIDE = BLOCK*W; // item size, distance of consecutive items
+// Slot-array addresses of one time step, computed on the host for each launch so that a slot
+// address in the kernel is one multiply-add of a per-thread index onto a kernel-parameter base
+// instead of a per-direction computation of fi + i N + e: a[0] = fi (rest slots); for each opposite
+// pair (i, i+1), i odd, a[i] = fi + i N + e (the array of the cells' own slots) and
+// a[i+1] = fi + (i+1) N - e (the array of their neighbours' slots), with e = 0 at odd t and N at
+// even t (the Esoteric-Pull slot map of src/kernel.cpp:1326-1339).
+struct SlotTable { const void* a[27]; };
+template<typename T> inline SlotTable slot_table(const StepArgs& s, const int q) {
+	SlotTable tb{};
+	const T* fi = (const T*)s.fi;
+	const uint64_t N = s.g.N, e = (s.t&1ull) ? 0ull : N;
+	tb.a[0] = fi;
+	for(int i=1; i<q; i+=2) { tb.a[i] = fi+((uint64_t)i*N+e); tb.a[i+1] = fi+((uint64_t)(i+1)*N-e); }
+	return tb;
+}
+template<int Q, int ST, typename T> __device__ __forceinline__ void issue_pair_t(const SlotTable& tb, const uint8_t* __restrict__ flags,
+                                                                                 const Steps32& sa, const Steps32& sb, const uint32_t s0) {
+	constexpr uint32_t W = 2u*sizeof(T), STRIDE = PIPE_BLOCK*W;
 	auto cpw = [](const uint32_t d, const T* p) { if constexpr(W==4u) cp_async_4(d, p); else cp_async_8(d, p); };
-	const uint64_t e = odd ? 0ull : N;
 	cp_async_4(s0, flags+(sa.n&~3u));
-	cpw(s0+STRIDE, fi+sa.n);
+	cpw(s0+STRIDE, (const T*)tb.a[0]+sa.n);
 	Unroll<1, Q, 2>::run([&](auto ic) {
 		constexpr int i = decltype(ic)::value;
 		constexpr uint32_t ka = 2u+(uint32_t)(i-1)/2u, kb = (uint32_t)pair_b_item<Q>(i);
-		const T* pa = fi+((uint64_t)i*N+e);
-		const T* pb = fi+((uint64_t)(i+1)*N-e);
+		const T* pa = (const T*)tb.a[i];
+		const T* pb = (const T*)tb.a[i+1];
 		cpw(s0+ka*STRIDE, pa+sa.n);
 		if constexpr(vs_c(0, i)==0) cpw(s0+kb*STRIDE, pb+sa.template j<i>());
 		else if constexpr(W==4u) { cp_async_4(s0+kb*STRIDE, pb+(sa.template j<i>()-1u)); cp_async_4(s0+(kb+1u)*STRIDE, pb+sb.template j<i>()); }
 		else { cp_async_4(s0+kb*STRIDE, pb+sa.template j<i>()); cp_async_4(s0+(kb+1u)*STRIDE, pb+sb.template j<i>()); }
 	});
 }
-
-// Byte offsets of both cells of a pair (x even, x+1) and of their neighbours at one z plane, for
-// lattices whose DDF arrays are under 4 GB each (N * sizeof(T) < 2^32). Steps carry the periodic wrap
-// as Steps32 does, in bytes; what differs from two Steps32 is what the pair's geometry fixes: with
-// Nx and x even, cell x+1 never wraps towards -x and cell x never towards +x, and both share their y
-// and z steps. Each access is a 64-bit uniform array base plus a 32-bit per-thread offset.
-template<int E> struct PairSteps {
-	uint32_t n, xm_a, xp_b, yp, ym, zp, zm;
-	__device__ __forceinline__ PairSteps(const Grid& g, const uint32_t x, const uint32_t y, const uint32_t z, const uint32_t n_) {
-		const uint32_t N = (uint32_t)g.N;
-		n = n_*(uint32_t)E;
-		xm_a = (x==0u ? g.Nx-1u : 0xFFFFFFFFu)*(uint32_t)E;
-		xp_b = (x+2u==g.Nx ? 1u-g.Nx : 1u)*(uint32_t)E;
-		yp = (y+1u==g.Ny ? g.Nx-g.NxNy : g.Nx)*(uint32_t)E;
-		ym = (y==0u ? g.NxNy-g.Nx : 0u-g.Nx)*(uint32_t)E;
-		zp = (z+1u==g.Nz ? g.NxNy-N : g.NxNy)*(uint32_t)E;
-		zm = (z==0u ? N-g.NxNy : 0u-g.NxNy)*(uint32_t)E;
-	}
-	template<int I> __device__ __forceinline__ uint32_t yz() const {
-		constexpr int b = vs_c(1, I), c = vs_c(2, I);
-		const uint32_t sy = b>0 ? yp : b<0 ? ym : 0u, sz = c>0 ? zp : c<0 ? zm : 0u;
-		return b!=0 && c!=0 ? sy+sz : b!=0 ? sy : c!=0 ? sz : 0u;
-	}
-	template<int I> __device__ __forceinline__ uint32_t ja() const { // neighbour of cell x along c_I
-		constexpr int a = vs_c(0, I);
-		return a>0 ? n+(uint32_t)E+yz<I>() : a<0 ? n+xm_a+yz<I>() : n+yz<I>();
-	}
-	template<int I> __device__ __forceinline__ uint32_t jb() const { // neighbour of cell x+1 along c_I
-		constexpr int a = vs_c(0, I);
-		return a>0 ? n+(uint32_t)E+xp_b+yz<I>() : a<0 ? n+yz<I>() : n+(uint32_t)E+yz<I>();
-	}
-};
-template<typename T> __device__ __forceinline__ const T* at(const T* base, const uint32_t off) { return (const T*)((const char*)base+off); }
-template<typename T> __device__ __forceinline__ T* at(T* base, const uint32_t off) { return (T*)((char*)base+off); }
-
-template<int Q, int ST, typename T> __device__ __forceinline__ void issue_pair_b(const T* __restrict__ fi, const uint8_t* __restrict__ flags, const uint64_t N,
-                                                                                 const PairSteps<sizeof(T)>& p, const uint32_t nc, const bool odd, const uint32_t s0) {
-	constexpr uint32_t W = 2u*sizeof(T), STRIDE = BLOCK*W;
-	auto cpw = [](const uint32_t d, const T* q) { if constexpr(W==4u) cp_async_4(d, q); else cp_async_8(d, q); };
-	const uint64_t e = odd ? 0ull : N;
-	cp_async_4(s0, flags+(nc&~3u));
-	cpw(s0+STRIDE, at(fi, p.n));
-	Unroll<1, Q, 2>::run([&](auto ic) {
-		constexpr int i = decltype(ic)::value;
-		constexpr uint32_t ka = 2u+(uint32_t)(i-1)/2u, kb = (uint32_t)pair_b_item<Q>(i);
-		const T* pa = fi+((uint64_t)i*N+e);
-		const T* pb = fi+((uint64_t)(i+1)*N-e);
-		cpw(s0+ka*STRIDE, at(pa, p.n));
-		if constexpr(vs_c(0, i)==0) cpw(s0+kb*STRIDE, at(pb, p.template ja<i>()));
-		else if constexpr(W==4u) { cp_async_4(s0+kb*STRIDE, at(pb, p.template ja<i>()-(uint32_t)sizeof(T))); cp_async_4(s0+(kb+1u)*STRIDE, at(pb, p.template jb<i>())); }
-		else { cp_async_4(s0+kb*STRIDE, at(pb, p.template ja<i>())); cp_async_4(s0+(kb+1u)*STRIDE, at(pb, p.template jb<i>())); }
-	});
-}
-template<int Q, int ST, typename T> __device__ __forceinline__ void store_pair_b(T* __restrict__ fi, const uint64_t N, const PairSteps<sizeof(T)>& p,
-                                                                                 const bool odd, const float2* f) {
+template<int Q, int ST, typename T> __device__ __forceinline__ void store_pair_t(const SlotTable& tb, const Steps32& sa, const Steps32& sb, const float2* f) {
 	typedef RawCodec<ST> CD;
-	const uint64_t e = odd ? 0ull : N;
-	PairIO<ST>::store2(at(fi, p.n), f[0]);
+	PairIO<ST>::store2((T*)tb.a[0]+sa.n, f[0]);
 	Unroll<1, Q, 2>::run([&](auto ic) {
 		constexpr int i = decltype(ic)::value;
-		T* pa = fi+((uint64_t)i*N+e);
-		T* pb = fi+((uint64_t)(i+1)*N-e);
-		if constexpr(vs_c(0, i)==0) PairIO<ST>::store2(at(pb, p.template ja<i>()), f[i]);
-		else { *at(pb, p.template ja<i>()) = CD::encode(f[i].x); *at(pb, p.template jb<i>()) = CD::encode(f[i].y); }
-		PairIO<ST>::store2(at(pa, p.n), f[i+1]);
+		T* pa = (T*)tb.a[i];
+		T* pb = (T*)tb.a[i+1];
+		if constexpr(vs_c(0, i)==0) PairIO<ST>::store2(pb+sa.template j<i>(), f[i]);
+		else { pb[sa.template j<i>()] = CD::encode(f[i].x); pb[sb.template j<i>()] = CD::encode(f[i].y); }
+		PairIO<ST>::store2(pa+sa.n, f[i+1]);
 	});
 }
 
-// the pair's values from its staged items (item k of this thread at w[k*BLOCK])
+// the pair's values from its staged items (item k of this thread at w[k*PIPE_BLOCK])
 template<int ST> struct PairStage;
 template<> struct PairStage<ST_FP32> {
 	typedef float2 W;
-	static __device__ __forceinline__ float2 pair(const W* w, const int k) { return w[k*BLOCK]; }
-	static __device__ __forceinline__ float2 split(const W* w, const int k) { return make_float2(w[k*BLOCK].x, w[(k+1)*BLOCK].x); }
+	static __device__ __forceinline__ float2 pair(const W* w, const int k) { return w[k*PIPE_BLOCK]; }
+	static __device__ __forceinline__ float2 split(const W* w, const int k) { return make_float2(w[k*PIPE_BLOCK].x, w[(k+1)*PIPE_BLOCK].x); }
 	static __device__ __forceinline__ uint32_t flags(const W* w) { return __float_as_uint(w[0].x); }
 };
 template<> struct PairStage<ST_FP16S> {
 	typedef uint32_t W;
-	static __device__ __forceinline__ float2 pair(const W* w, const int k) { return __half22float2(__halves2half2(__ushort_as_half((uint16_t)(w[k*BLOCK]&0xFFFFu)), __ushort_as_half((uint16_t)(w[k*BLOCK]>>16)))); }
+	static __device__ __forceinline__ float2 pair(const W* w, const int k) { return __half22float2(__halves2half2(__ushort_as_half((uint16_t)(w[k*PIPE_BLOCK]&0xFFFFu)), __ushort_as_half((uint16_t)(w[k*PIPE_BLOCK]>>16)))); }
 	static __device__ __forceinline__ float2 split(const W* w, const int k) { // upper half of item k, lower half of item k+1
-		const uint32_t v = __byte_perm(w[k*BLOCK], w[(k+1)*BLOCK], 0x5432u);
+		const uint32_t v = __byte_perm(w[k*PIPE_BLOCK], w[(k+1)*PIPE_BLOCK], 0x5432u);
 		return __half22float2(__halves2half2(__ushort_as_half((uint16_t)(v&0xFFFFu)), __ushort_as_half((uint16_t)(v>>16))));
 	}
 	static __device__ __forceinline__ uint32_t flags(const W* w) { return w[0]; }
 };
 template<> struct PairStage<ST_FP16C> { // the two codes read as 16-bit halves of the staged words
 	typedef uint32_t W;
-	static __device__ __forceinline__ const uint16_t* h(const W* w, const int k) { return reinterpret_cast<const uint16_t*>(w+k*BLOCK); }
+	static __device__ __forceinline__ const uint16_t* h(const W* w, const int k) { return reinterpret_cast<const uint16_t*>(w+k*PIPE_BLOCK); }
 	static __device__ __forceinline__ float2 pair(const W* w, const int k) { return make_float2(RawCodec<ST_FP16C>::decode(h(w, k)[0]), RawCodec<ST_FP16C>::decode(h(w, k)[1])); }
 	static __device__ __forceinline__ float2 split(const W* w, const int k) { return make_float2(RawCodec<ST_FP16C>::decode(h(w, k)[1]), RawCodec<ST_FP16C>::decode(h(w, k+1)[0])); }
 	static __device__ __forceinline__ uint32_t flags(const W* w) { return w[0]; }
@@ -431,33 +398,27 @@ template<int Q, int ST> __device__ __forceinline__ void read_pair(const typename
 	});
 }
 
-#ifndef FX3D_PIPE_MIN_BLOCKS
-#define FX3D_PIPE_MIN_BLOCKS 3
-#endif
-#ifndef FX3D_PIPE_BYTE_OFFSETS
-#define FX3D_PIPE_BYTE_OFFSETS 0
-#endif
-#ifndef FX3D_PIPE_REREAD
-#define FX3D_PIPE_REREAD 0
+#ifndef FX3D_PIPE_MIN_THREADS
+#define FX3D_PIPE_MIN_THREADS 768 // resident threads per SM the register budget is sized for
 #endif
 #ifndef FX3D_PIPE_STAGES
 #define FX3D_PIPE_STAGES 2
 #endif
 #ifndef FX3D_PIPE_Z_CHUNK
-#define FX3D_PIPE_Z_CHUNK 8
+#define FX3D_PIPE_Z_CHUNK 2
 #endif
 constexpr int PIPE_STAGES = FX3D_PIPE_STAGES; // pairs in flight per thread: PIPE_STAGES-1 ahead of the one stepped
 inline uint32_t pipe_z_chunk(const GridDesc& g) { return g.Nz<(uint32_t)FX3D_PIPE_Z_CHUNK ? g.Nz : (uint32_t)FX3D_PIPE_Z_CHUNK; } // z planes per thread
-template<int Q, int ST> inline size_t pipe_smem(const int stages) { return (size_t)stages*pair_items<Q>()*BLOCK*2u*sizeof(typename Codec<ST>::T); }
+template<int Q, int ST> inline size_t pipe_smem(const int stages) { return (size_t)stages*pair_items<Q>()*PIPE_BLOCK*2u*sizeof(typename Codec<ST>::T); }
 
-template<int Q, int ST, bool TRT, int EXT, int S> __global__ void __launch_bounds__(BLOCK, ((EXT&EXT_SG)!=0 ? 2 : FX3D_PIPE_MIN_BLOCKS)) k_stream_collide_pairs_pipe(const StepArgs a, const uint32_t zc) {
+template<int Q, int ST, bool TRT, int EXT, int S> __global__ void __launch_bounds__(PIPE_BLOCK, ((EXT&EXT_SG)!=0 ? 512 : FX3D_PIPE_MIN_THREADS)/PIPE_BLOCK) k_stream_collide_pairs_pipe(const StepArgs a, const uint32_t zc, const SlotTable tb) {
 	typedef typename Codec<ST>::T T;
 	typedef typename PairStage<ST>::W SW;
 	constexpr bool EQ = (EXT&EXT_EQ)!=0, VF = (EXT&EXT_VF)!=0;
 	constexpr int ITEMS = pair_items<Q>();
 	extern __shared__ __align__(16) uint8_t pipe_smem_raw[];
 	const Grid& g = grid_of(a.g);
-	const uint32_t xy = 2u*(blockIdx.x*(uint32_t)BLOCK+threadIdx.x);
+	const uint32_t xy = 2u*(blockIdx.x*(uint32_t)PIPE_BLOCK+threadIdx.x);
 	if(xy>=g.NxNy) return; // threads never wait on each other
 	const uint32_t y = div_nx(g, xy), x = xy-y*g.Nx;
 	const uint32_t z0 = blockIdx.y*zc, z1 = min(z0+zc, g.Nz);
@@ -466,12 +427,8 @@ template<int Q, int ST, bool TRT, int EXT, int S> __global__ void __launch_bound
 	const uint32_t s0 = smem_u32(w0);
 	auto issue = [&](const uint32_t z, const int stage) {
 		const uint32_t n = z*g.NxNy+xy;
-#if FX3D_PIPE_BYTE_OFFSETS
-		issue_pair_b<Q, ST>((const T*)a.fi, a.flags, g.N, PairSteps<sizeof(T)>(g, x, y, z, n), n, odd, s0+(uint32_t)(stage*ITEMS*BLOCK)*(uint32_t)sizeof(SW));
-#else
 		const Steps32 sa(g, x, y, z, n), sb(g, x+1u, y, z, n+1u);
-		issue_pair<Q, ST>((const T*)a.fi, a.flags, g.N, sa, sb, odd, s0+(uint32_t)(stage*ITEMS*BLOCK)*(uint32_t)sizeof(SW));
-#endif
+		issue_pair_t<Q, ST, T>(tb, a.flags, sa, sb, s0+(uint32_t)(stage*ITEMS*PIPE_BLOCK)*(uint32_t)sizeof(SW));
 	};
 	#pragma unroll
 	for(int s=0; s<S-1; s++) {
@@ -484,7 +441,7 @@ template<int Q, int ST, bool TRT, int EXT, int S> __global__ void __launch_bound
 		if(z+(uint32_t)(S-1)<z1) issue(z+(uint32_t)(S-1), ahead);
 		cp_async_commit();
 		cp_async_wait<S-1>();
-		const SW* w = w0+stage*ITEMS*BLOCK;
+		const SW* w = w0+stage*ITEMS*PIPE_BLOCK;
 		stage = stage+1<S ? stage+1 : 0;
 		const uint32_t n = z*g.NxNy+xy;
 		const uint32_t fl = PairStage<ST>::flags(w)>>((n&3u)*8u); // both cells' flags (n even)
@@ -522,25 +479,15 @@ template<int Q, int ST, bool TRT, int EXT, int S> __global__ void __launch_bound
 			store_f32<Q, RawCodec<ST>>((T*)a.fi, g.N, s, odd, f1);
 			continue;
 		}
-#if !FX3D_PIPE_BYTE_OFFSETS
 		const Steps32 sa(g, x, y, z, n), sb(g, x+1u, y, z, n+1u);
-#endif
 		const Bool2 is_e{EQ && (fa&TYPE_BO)==TYPE_E, EQ && (fb&TYPE_BO)==TYPE_E};
 		const bool any_e = is_e.x||is_e.y;
 		float2 R, Rm1, inv, ux, uy, uz, fx, fy, fz;
 		cell_rho_u_v<Q, EXT, ST, float2>(a, n, f, is_e, any_e, R, Rm1, inv, ux, uy, uz, fx, fy, fz);
 		if(a.fields_out) store_pair_fields<ST>(a, n, R, ux, uy, uz, is_e, any_e);
-		if constexpr(FX3D_PIPE_REREAD!=0) { // read the staged values again instead of holding them through the moments
-			asm volatile("" ::: "memory");
-			read_pair<Q, ST>(w, f);
-		}
 		if(any_e) collide_v<Q, TRT, VF, ST, 2, float2, Bool2, (EXT&EXT_SG)!=0>(f, R, Rm1, ux, uy, uz, fx, fy, fz, is_e, a);
 		else collide_v<Q, TRT, VF, ST, 0, float2, Bool2, (EXT&EXT_SG)!=0>(f, R, Rm1, ux, uy, uz, fx, fy, fz, is_e, a);
-#if FX3D_PIPE_BYTE_OFFSETS
-		store_pair_b<Q, ST>((T*)a.fi, g.N, PairSteps<sizeof(T)>(g, x, y, z, n), odd, f);
-#else
-		store_pair<Q, ST>((T*)a.fi, g.N, sa, sb, odd, f);
-#endif
+		store_pair_t<Q, ST, T>(tb, sa, sb, f);
 	}
 }
 
@@ -760,7 +707,7 @@ template<int ST, int Q, bool TRT, int EXT, bool FAST> inline cudaError_t sc_laun
 					if(e!=cudaSuccess) return e;
 				}
 				const uint32_t zc = pipe_z_chunk(a.g);
-				kernel<<<dim3(pair_grid(a.g).x, (a.g.Nz+zc-1u)/zc, 1u), BLOCK, smem, s>>>(a, zc);
+				kernel<<<dim3((a.g.NxNy/2u+PIPE_BLOCK-1u)/PIPE_BLOCK, (a.g.Nz+zc-1u)/zc, 1u), PIPE_BLOCK, smem, s>>>(a, zc, slot_table<typename Codec<ST>::T>(a, Q));
 			}
 		} else {
 			return cudaErrorInvalidConfiguration; // the packed kernel has fast arithmetic only
