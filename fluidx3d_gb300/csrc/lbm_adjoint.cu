@@ -2,9 +2,13 @@
 // the reference). One forward step maps the slots of each fluid cell (its Esoteric-Pull slot set at
 // the step's parity) to themselves: gather g (load_f), h = Phi(g; F), scatter h (store_f). Its
 // adjoint is therefore local and in place, with the forward kernel's memory pattern: lambda is read
-// at the store positions (hbar), the cell recomputes its forward quantities from the saved state f^k
-// and writes gbar = (dPhi/dg)^T hbar (+ dj_k/dg of the objective) at the load positions; solid cells
-// map their slots identically. grad accumulates (dPhi/dF)^T hbar plus the objective's direct F term.
+// at the store positions (hbar), the cell takes its forward quantities from the moment checkpoint of
+// step k and writes gbar = (dPhi/dg)^T hbar (+ dj_k/dg of the objective) at the load positions; solid
+// cells map their slots identically. grad accumulates (dPhi/dF)^T hbar plus the objective's direct F
+// term. dPhi/dg depends on g only through rho and u0 = m/rho (the collision is affine in g at fixed
+// rho, u), so the 16 bytes of (rho, u) that the forward step writes per cell (its fused-fields output)
+// replace the saved DDFs: with v = u0 + Ft/(2 rho) and u = clamp(v), v is inside the clamp range
+// exactly when |u| < c, and then u0 = u - Ft/(2 rho) (u0 is not needed where the clamp is active).
 //
 // The chain (forward in lbm_scheme.cuh, reference src/kernel.cpp:1454-1636):
 //   rho = sum g + 1, m = sum c g, u0 = m/rho, v = u0 + Ft/(2 rho), u = clamp(v), Ft = (fx,fy,fz) + F
@@ -50,6 +54,20 @@ template<int Q, bool VF> __device__ __forceinline__ void adj_forward(const float
 		const float v = VF ? fmaf(Ft[d], s.rho2, s.u0[d]) : s.u0[d];
 		s.kappa[d] = v>-DEF_C && v<DEF_C;
 		s.u[d] = clampc(v);
+	}
+	s.c3 = -3.0f*fmaf(s.u[0], s.u[0], fmaf(s.u[1], s.u[1], s.u[2]*s.u[2]));
+}
+
+// the same from the fields a forward step collides a fluid cell with: rho and u = clamp(u0 + Ft/(2 rho))
+template<int Q, bool VF> __device__ __forceinline__ void adj_from_fields(const float rho, const float* u, const float* Ft, CellState<Q>& s) {
+	s.rho = rho;
+	s.rho2 = 0.5f*v_rcp(rho);
+	#pragma unroll
+	for(int d=0; d<3; d++) {
+		s.Ft[d] = Ft[d];
+		s.u[d] = u[d];
+		s.kappa[d] = u[d]>-DEF_C && u[d]<DEF_C;
+		s.u0[d] = VF ? fmaf(-Ft[d], s.rho2, u[d]) : u[d];
 	}
 	s.c3 = -3.0f*fmaf(s.u[0], s.u[0], fmaf(s.u[1], s.u[1], s.u[2]*s.u[2]));
 }
@@ -230,12 +248,21 @@ template<int Q, int ST, bool TRT, int EXT, bool OBJ_ONLY> __global__ void __laun
 	}
 	CellState<Q> s;
 	{
-		float gv[Q];
-		load_f32<Q, Codec<ST>>((const T*)j.state, N, st, odd, gv);
 		float Ft[3] = {a.fx, a.fy, a.fz};
 		if constexpr(FF) { Ft[0] += a.F[n]; Ft[1] += a.F[N+n]; Ft[2] += a.F[2ull*N+n]; }
-		const float up[3] = {is_e ? a.u[n] : 0.0f, is_e ? a.u[N+n] : 0.0f, is_e ? a.u[2ull*N+n] : 0.0f};
-		adj_forward<Q, VF>(gv, is_e, is_e ? a.rho[n] : 1.0f, up, Ft, s);
+		if(is_e) { // the presets
+			const float up[3] = {a.u[n], a.u[N+n], a.u[2ull*N+n]};
+			adj_forward<Q, VF>(nullptr, true, a.rho[n], up, Ft, s);
+		} else if constexpr(OBJ_ONLY) { // the final state (no step left to write its moments): from its DDFs
+			float gv[Q];
+			load_f32<Q, Codec<ST>>((const T*)j.state, N, st, odd, gv);
+			const float up[3] = {0.0f, 0.0f, 0.0f};
+			adj_forward<Q, VF>(gv, false, 1.0f, up, Ft, s);
+		} else {
+			const float* M = j.moments;
+			const float uf[3] = {M[N+n], M[2ull*N+n], M[3ull*N+n]};
+			adj_from_fields<Q, VF>(M[n], uf, Ft, s);
+		}
 	}
 	float Fbar[3] = {0.0f, 0.0f, 0.0f};
 	// gbar of direction k goes to the load position of g_k: n (k = 0), A_i (k = i odd), B_i (k = i+1)

@@ -6,7 +6,9 @@ namespace fx3d {
 
 enum : int { OBJ_KE_PLANE = 1, OBJ_DRAG_X = 2 };
 struct AdjArgs {
-	const void* state; // f^k, DDFs before step k, in the domain's storage format
+	const void* state; // f^k, DDFs before step k, in the domain's storage format (objective terms)
+	const float* moments; // rho[N] then u[3N] of f^k as step k collides with them (force-shifted, clamped
+	                      // velocity; not written at TYPE_E cells, whose presets are a.rho/a.u): the adjoint step's input
 	float* lambda;     // q*N adjoint DDFs (FP32), updated in place
 	float* grad;       // 3N dJ/dF accumulator
 	int obj_kind;

@@ -73,6 +73,7 @@ struct lbm_domain {
 		a.t = t; a.fx = cfg.fx; a.fy = cfg.fy; a.fz = cfg.fz; a.w = w;
 		a.err = err;
 		a.fields_out = fused_fields ? 1 : 0;
+		a.rho_out = rho; a.u_out = u;
 		a.omw = rates.omw; a.c_tau = rates.c_tau; a.hp = rates.hp; a.hm = rates.hm; a.c_taup = rates.c_taup; a.c_taum = rates.c_taum;
 		return a;
 	}
@@ -672,27 +673,19 @@ struct DeviceBuffer { // freed on scope exit
 	~DeviceBuffer() { if(p) cudaFree(p); }
 };
 
-// f^{k+1} = step(f^k) from src into dst: one thread per cell steps out of place (the row-staged
-// kernel when that path is forced); the two-cell kernels step in place only, so with one of those
-// forced the state is copied first
-int step_out_of_place(lbm_domain* d, const void* src, void* dst, const uint64_t t, cudaStream_t stream) {
+// one forward step in place on a work copy of the DDFs that also writes the rho/u its cells collide
+// with (its fused-fields output) into a moment checkpoint: rho at mom[0, N), u at mom[N, 4N)
+int step_with_moments(lbm_domain* d, void* work, float* mom, const uint64_t t, cudaStream_t stream) {
 	StepArgs a = d->args();
 	a.t = t;
-	a.fields_out = 0; // recomputed states leave the fields of the forward run alone
-	const bool rows_ok = row_plan(d->v.q, d->v.storage, d->g.Nx, d->g.Ny, d->g.Nz).stages!=0u;
-	int path = d->path==PATH_ROWS && rows_ok ? PATH_ROWS : PATH_CELLS;
-	if(d->path==PATH_PAIRS||d->path==PATH_PIPE) {
-		FX3D_CUDA(cudaMemcpyAsync(dst, src, d->field_bytes(LBM_FIELD_FI), cudaMemcpyDeviceToDevice, stream), "cudaMemcpyAsync(state)");
-		a.fi = dst; a.fi_dst = dst;
-		path = d->path;
-	} else {
-		a.fi = const_cast<void*>(src); a.fi_dst = dst;
-	}
+	a.fi = work; a.fi_dst = work;
+	a.fields_out = mom ? 1 : 0;
+	if(mom) { a.rho_out = mom; a.u_out = mom+d->g.N; }
 	cudaError_t e;
 	switch(d->v.storage) {
-		case ST_FP32: e = launch_stream_collide_fp32(d->v, a, path, stream); break;
-		case ST_FP16S: e = launch_stream_collide_fp16s(d->v, a, path, stream); break;
-		default: e = launch_stream_collide_fp16c(d->v, a, path, stream); break;
+		case ST_FP32: e = launch_stream_collide_fp32(d->v, a, d->path, stream); break;
+		case ST_FP16S: e = launch_stream_collide_fp16s(d->v, a, d->path, stream); break;
+		default: e = launch_stream_collide_fp16c(d->v, a, d->path, stream); break;
 	}
 	return e==cudaSuccess ? LBM_OK : cuda_fail(e, "stream_collide (recompute)");
 }
@@ -745,37 +738,42 @@ extern "C" int lbm_run_adjoint(lbm_domain* d, const lbm_adjoint_config* cfg, dou
 		if(cells==0ull) return fail(LBM_ERR_INVALID_ARGUMENT, "lbm_run_adjoint: plane x=%u has no fluid cells", cfg->plane_x);
 		weight /= (double)cells;
 	}
-	// workspace: snapshots, segment states (all of a segment, or sub-snapshots + a sub-segment), lambda, gradient, J
+	// workspace: DDF snapshots every K steps, one work copy of the DDFs for the recomputation, and
+	// moment checkpoints (rho/u, 16 B per cell) of every step of a segment; with room for two moment
+	// sets the recomputation of the next segment runs on a second stream while the adjoint steps of
+	// this one run. Short of room for one set, two levels: DDF sub-snapshots every K2 steps of a
+	// segment, and moments of one sub-segment.
 	size_t free_b = 0u, total_b = 0u;
 	FX3D_CUDA(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo");
+	const size_t MB = N*16u; // moments of one step
 	const size_t fixed = (size_t)d->cfg.velocity_set*N*4u+N*12u+64u;
 	const size_t margin = 512ull<<20;
-	uint64_t K2 = K; // states kept per (sub-)segment
+	uint64_t K2 = K; // steps per (sub-)segment with moments
 	uint32_t levels = 1u;
-	// one level: a segment's states after its snapshot (K-1); with room for two such buffers the
-	// recomputation of the next segment runs on a second stream while the adjoint steps of this one run
-	size_t need = (nsnap+2ull*(K-1ull))*SB+fixed;
-	bool overlap = K>1ull && nsnap>1ull && need+margin<=free_b;
-	if(!overlap) need = (nsnap+K)*SB+fixed;
+	size_t need = (nsnap+1ull)*SB+2ull*K*MB+fixed;
+	bool overlap = nsnap>1ull && need+margin<=free_b;
+	if(!overlap) need = (nsnap+1ull)*SB+K*MB+fixed;
 	if(need+margin>free_b) {
 		levels = 2u;
-		K2 = 2ull; while(K2*K2<K) K2++; // >= 2: the recomputation ping-pongs between two states
-		need = (nsnap+(K+K2-1ull)/K2+K2)*SB+fixed;
+		K2 = 1ull; while(K2*K2<K) K2++;
+		need = (nsnap+1ull+(K+K2-1ull)/K2)*SB+K2*MB+fixed;
 		if(need+margin>free_b) return fail(LBM_ERR_OUT_OF_MEMORY, "lbm_run_adjoint: %zu MB of workspace needed, %zu MB free; increase checkpoint_interval", need>>20, free_b>>20);
 	}
 	const uint64_t nsub = levels==2u ? (K+K2-1ull)/K2 : 0ull;
-	DeviceBuffer snaps, seg, sub, lam, grad, Jd;
+	DeviceBuffer snaps, work, moms, sub, lam, grad, Jd;
 	FX3D_CUDA(cudaMalloc(&snaps.p, (size_t)nsnap*SB), "cudaMalloc(snapshots)");
-	FX3D_CUDA(cudaMalloc(&seg.p, (size_t)(overlap ? 2ull*(K-1ull) : K2)*SB), "cudaMalloc(segment states)");
+	FX3D_CUDA(cudaMalloc(&work.p, SB), "cudaMalloc(recomputation state)");
+	FX3D_CUDA(cudaMalloc(&moms.p, (size_t)(overlap ? 2ull*K : K2)*MB), "cudaMalloc(moment checkpoints)");
 	if(levels==2u) FX3D_CUDA(cudaMalloc(&sub.p, (size_t)nsub*SB), "cudaMalloc(sub-snapshots)");
 	FX3D_CUDA(cudaMalloc(&lam.p, (size_t)d->cfg.velocity_set*N*4u), "cudaMalloc(adjoint DDFs)");
 	FX3D_CUDA(cudaMalloc(&grad.p, N*12u), "cudaMalloc(gradient)");
 	FX3D_CUDA(cudaMalloc(&Jd.p, sizeof(double)), "cudaMalloc(J)");
 	auto snap = [&](const uint64_t i) { return (void*)((char*)snaps.p+(size_t)i*SB); };
-	auto segs = [&](const uint64_t i) { return (void*)((char*)seg.p+(size_t)i*SB); };
+	auto mom = [&](const uint64_t set, const uint64_t i) { return (float*)((char*)moms.p+((size_t)set*K+(size_t)i)*MB); };
 	auto subs = [&](const uint64_t i) { return (void*)((char*)sub.p+(size_t)i*SB); };
 	AdjArgs j;
 	j.lambda = (float*)lam.p; j.grad = (float*)grad.p; j.obj_kind = (int)cfg->objective; j.plane_x = cfg->plane_x; j.marker = cfg->marker;
+	j.moments = nullptr;
 	auto in_window = [&](const uint64_t t) { return t>=cfg->window_begin && t<=cfg->window_end; };
 	auto args_at = [&](const uint64_t t, const void* state) { StepArgs a = d->args(); a.t = t; a.fi = const_cast<void*>(state); return a; };
 
@@ -799,69 +797,66 @@ extern "C" int lbm_run_adjoint(lbm_domain* d, const lbm_adjoint_config* cfg, dou
 		j.state = d->fi; j.obj_weight = (float)weight;
 		FX3D_CUDA(launch_adjoint_step(d->v, args_at(t0+T, d->fi), j, true, d->stream), "adjoint objective");
 	}
-	auto reverse_states = [&](const uint64_t k0, const uint64_t k1, const void* start) -> int { // adjoint of steps k1-1 .. k0 from f^{k0} = start
-		EventTimer tr(d->stream);
-		FX3D_CUDA(cudaMemcpyAsync(segs(0), start, SB, cudaMemcpyDeviceToDevice, d->stream), "cudaMemcpyAsync(state)");
-		for(uint64_t k=k0; k+1ull<k1; k++) { const int r = step_out_of_place(d, segs(k-k0), segs(k-k0+1ull), t0+k, d->stream); if(r!=LBM_OK) return r; }
-		recompute_ms += tr.stop(d->stream);
-		EventTimer ta(d->stream);
+	// moments of steps k0 .. k1-1 into set `set`, from the DDF state f^{k0} at `start` (work copy)
+	auto recompute = [&](const uint64_t k0, const uint64_t k1, const void* start, const uint64_t set, cudaStream_t st) -> int {
+		FX3D_CUDA(cudaMemcpyAsync(work.p, start, SB, cudaMemcpyDeviceToDevice, st), "cudaMemcpyAsync(state)");
+		for(uint64_t k=k0; k<k1; k++) { const int r = step_with_moments(d, work.p, mom(set, k-k0), t0+k, st); if(r!=LBM_OK) return r; }
+		return LBM_OK;
+	};
+	auto adjoint_steps = [&](const uint64_t k0, const uint64_t k1, const uint64_t set) -> int { // steps k1-1 .. k0
 		for(uint64_t k=k1; k-->k0;) {
-			j.state = segs(k-k0); j.obj_weight = in_window(t0+k) ? (float)weight : 0.0f;
-			FX3D_CUDA(launch_adjoint_step(d->v, args_at(t0+k, j.state), j, false, d->stream), "adjoint step");
+			j.moments = mom(set, k-k0); j.state = nullptr; j.obj_weight = in_window(t0+k) ? (float)weight : 0.0f;
+			FX3D_CUDA(launch_adjoint_step(d->v, args_at(t0+k, nullptr), j, false, d->stream), "adjoint step");
 		}
-		adjoint_ms += ta.stop(d->stream);
 		return LBM_OK;
 	};
 	EventTimer trev(d->stream);
 	StreamAndEvents ov;
 	if(overlap) {
-		// segment s uses buffer s%2 for its states k0+1 .. k1-1 (its first state is the snapshot itself).
-		// Stream R recomputes segment s-1 while the domain's stream runs the adjoint steps of segment s;
-		// R waits until the adjoint steps of segment s+1 have released the buffer it refills.
+		// segment s uses moment set s%2. Stream R recomputes segment s-1 while the domain's stream runs
+		// the adjoint steps of segment s; R waits until the adjoint steps of segment s+1 have released
+		// the set it refills. The work copy of the DDFs belongs to stream R alone.
 		FX3D_CUDA(cudaStreamCreateWithFlags(&ov.stream, cudaStreamNonBlocking), "cudaStreamCreate");
 		for(cudaEvent_t& e : ov.ev) FX3D_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
 		cudaEvent_t* rec_done = ov.ev; cudaEvent_t* adj_done = ov.ev+2; cudaEvent_t start = ov.ev[4];
-		auto state = [&](const uint64_t sg, const uint64_t k) -> void* {
-			const uint64_t k0 = sg*K;
-			return k==k0 ? snap(sg) : (void*)((char*)seg.p+((size_t)(sg&1ull)*(K-1ull)+(size_t)(k-k0-1ull))*SB);
-		};
-		auto recompute = [&](const uint64_t sg, const bool wait_buffer) -> int {
+		auto recompute_segment = [&](const uint64_t sg, const bool wait_set) -> int {
 			const uint64_t k0 = sg*K, k1 = std::min<uint64_t>(k0+K, T);
-			if(wait_buffer) FX3D_CUDA(cudaStreamWaitEvent(ov.stream, adj_done[sg&1ull], 0), "cudaStreamWaitEvent");
-			for(uint64_t k=k0; k+1ull<k1; k++) { const int r = step_out_of_place(d, state(sg, k), state(sg, k+1ull), t0+k, ov.stream); if(r!=LBM_OK) return r; }
+			if(wait_set) FX3D_CUDA(cudaStreamWaitEvent(ov.stream, adj_done[sg&1ull], 0), "cudaStreamWaitEvent");
+			{ const int r = recompute(k0, k1, snap(sg), sg&1ull, ov.stream); if(r!=LBM_OK) return r; }
 			FX3D_CUDA(cudaEventRecord(rec_done[sg&1ull], ov.stream), "cudaEventRecord");
 			return LBM_OK;
 		};
 		FX3D_CUDA(cudaEventRecord(start, d->stream), "cudaEventRecord");
 		FX3D_CUDA(cudaStreamWaitEvent(ov.stream, start, 0), "cudaStreamWaitEvent"); // after lambda/grad are cleared
-		{ const int r = recompute(nsnap-1ull, false); if(r!=LBM_OK) return r; }
+		{ const int r = recompute_segment(nsnap-1ull, false); if(r!=LBM_OK) return r; }
 		for(uint64_t sg=nsnap; sg-->0ull;) {
 			const uint64_t k0 = sg*K, k1 = std::min<uint64_t>(k0+K, T);
-			if(sg>=1ull) { const int r = recompute(sg-1ull, sg+1ull<nsnap); if(r!=LBM_OK) return r; }
+			if(sg>=1ull) { const int r = recompute_segment(sg-1ull, sg+1ull<nsnap); if(r!=LBM_OK) return r; }
 			FX3D_CUDA(cudaStreamWaitEvent(d->stream, rec_done[sg&1ull], 0), "cudaStreamWaitEvent");
-			for(uint64_t k=k1; k-->k0;) {
-				j.state = state(sg, k); j.obj_weight = in_window(t0+k) ? (float)weight : 0.0f;
-				FX3D_CUDA(launch_adjoint_step(d->v, args_at(t0+k, j.state), j, false, d->stream), "adjoint step");
-			}
+			{ const int r = adjoint_steps(k0, k1, sg&1ull); if(r!=LBM_OK) return r; }
 			FX3D_CUDA(cudaEventRecord(adj_done[sg&1ull], d->stream), "cudaEventRecord");
 		}
 	}
 	for(uint64_t s=nsnap; !overlap && s-->0ull;) {
 		const uint64_t k0 = s*K, k1 = std::min<uint64_t>(k0+K, T);
-		if(levels==1u) { const int r = reverse_states(k0, k1, snap(s)); if(r!=LBM_OK) return r; continue; }
-		// two levels: sub-snapshots every K2 steps of the segment, then each sub-segment in reverse
-		EventTimer tr(d->stream);
-		FX3D_CUDA(cudaMemcpyAsync(subs(0), snap(s), SB, cudaMemcpyDeviceToDevice, d->stream), "cudaMemcpyAsync(sub-snapshot)");
-		FX3D_CUDA(cudaMemcpyAsync(segs(0), snap(s), SB, cudaMemcpyDeviceToDevice, d->stream), "cudaMemcpyAsync(state)");
-		for(uint64_t k=k0; k+1ull<k1; k++) {
-			void* a0 = segs((k-k0)%2ull); void* a1 = segs((k-k0+1ull)%2ull);
-			const int r = step_out_of_place(d, a0, a1, t0+k, d->stream); if(r!=LBM_OK) return r;
-			if((k+1ull-k0)%K2==0ull) FX3D_CUDA(cudaMemcpyAsync(subs((k+1ull-k0)/K2), a1, SB, cudaMemcpyDeviceToDevice, d->stream), "cudaMemcpyAsync(sub-snapshot)");
+		if(levels==2u) { // DDF sub-snapshots every K2 steps of the segment
+			EventTimer tr(d->stream);
+			FX3D_CUDA(cudaMemcpyAsync(work.p, snap(s), SB, cudaMemcpyDeviceToDevice, d->stream), "cudaMemcpyAsync(state)");
+			for(uint64_t k=k0; k<k1; k++) {
+				if((k-k0)%K2==0ull) FX3D_CUDA(cudaMemcpyAsync(subs((k-k0)/K2), work.p, SB, cudaMemcpyDeviceToDevice, d->stream), "cudaMemcpyAsync(sub-snapshot)");
+				if(k+1ull<k1) { const int r = step_with_moments(d, work.p, nullptr, t0+k, d->stream); if(r!=LBM_OK) return r; }
+			}
+			recompute_ms += tr.stop(d->stream);
 		}
-		recompute_ms += tr.stop(d->stream);
-		for(uint64_t b=(k1-k0+K2-1ull)/K2; b-->0ull;) {
-			const int r = reverse_states(k0+b*K2, std::min<uint64_t>(k0+(b+1ull)*K2, k1), subs(b));
-			if(r!=LBM_OK) return r;
+		const uint64_t nb = levels==2u ? (k1-k0+K2-1ull)/K2 : 1ull;
+		for(uint64_t b=nb; b-->0ull;) {
+			const uint64_t b0 = levels==2u ? k0+b*K2 : k0, b1 = levels==2u ? std::min<uint64_t>(k0+(b+1ull)*K2, k1) : k1;
+			EventTimer tr(d->stream);
+			{ const int r = recompute(b0, b1, levels==2u ? subs(b) : snap(s), 0ull, d->stream); if(r!=LBM_OK) return r; }
+			recompute_ms += tr.stop(d->stream);
+			EventTimer ta(d->stream);
+			{ const int r = adjoint_steps(b0, b1, 0ull); if(r!=LBM_OK) return r; }
+			adjoint_ms += ta.stop(d->stream);
 		}
 	}
 	const double reverse_ms = trev.stop(d->stream);

@@ -35,6 +35,8 @@ struct StepArgs {
 	float fx, fy, fz, w;
 	int* err; // device error word (KERR_*), set by kernels whose bounded waits time out
 	int fields_out; // UPDATE_FIELDS: stream_collide writes the rho/u each cell collides with (not at TYPE_E cells with EQUILIBRIUM_BOUNDARIES)
+	float* rho_out; // where those fields go: rho and u (the domain's own, or per-step moment checkpoints of the adjoint)
+	float* u_out;
 	// collision rates derived from w on the host with the reference's FP32 operations
 	// (src/kernel.cpp:1598, 1606-1609): 1-w, fma(w,-0.5,1), 0.5*w, 0.5*wm, fma(w,-0.25,0.5), fma(wm,-0.25,0.5)
 	float omw, c_tau, hp, hm, c_taup, c_taum;

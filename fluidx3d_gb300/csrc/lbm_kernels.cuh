@@ -118,12 +118,12 @@ template<int Q, int EXT> __device__ __forceinline__ void cell_rho_u(const StepAr
 // cell collides with, written to rho/u; V = float2 writes cells n and n+1 (n even) as aligned pairs
 __device__ __forceinline__ void store_fields(const StepArgs& a, const uint64_t n, const float rho, const float ux, const float uy, const float uz) {
 	const uint64_t N = a.g.N;
-	a.rho[n] = rho; a.u[n] = ux; a.u[N+n] = uy; a.u[2ull*N+n] = uz;
+	a.rho_out[n] = rho; a.u_out[n] = ux; a.u_out[N+n] = uy; a.u_out[2ull*N+n] = uz;
 }
 __device__ __forceinline__ void store_fields(const StepArgs& a, const uint64_t n, const float2 rho, const float2 ux, const float2 uy, const float2 uz) {
 	const uint64_t N = a.g.N;
-	*reinterpret_cast<float2*>(a.rho+n) = rho; *reinterpret_cast<float2*>(a.u+n) = ux;
-	*reinterpret_cast<float2*>(a.u+N+n) = uy; *reinterpret_cast<float2*>(a.u+2ull*N+n) = uz;
+	*reinterpret_cast<float2*>(a.rho_out+n) = rho; *reinterpret_cast<float2*>(a.u_out+n) = ux;
+	*reinterpret_cast<float2*>(a.u_out+N+n) = uy; *reinterpret_cast<float2*>(a.u_out+2ull*N+n) = uz;
 }
 
 // one cell step on registers: f in, f out (exact: real units; fast: storage units)

@@ -187,8 +187,9 @@ typedef struct lbm_adjoint_stats {
 	double forward_ms;            /* device time of the forward sweep (steps, snapshots, objective) */
 	double recompute_ms, adjoint_ms; /* device time of the recomputation and of the adjoint steps when they run one
 	                               * after the other; 0 when they overlap (overlapped = 1): then see reverse_ms */
-	uint64_t workspace_bytes;     /* snapshots + recomputed states + adjoint DDFs + gradient */
-	uint32_t levels;              /* 1: every state of a segment kept; 2: sub-snapshots inside segments */
+	uint64_t workspace_bytes;     /* snapshots + recomputation state + moment checkpoints (rho/u, 16 B per cell and
+	                               * step) + adjoint DDFs + gradient */
+	uint32_t levels;              /* 1: moments of every step of a segment kept; 2: DDF sub-snapshots inside segments */
 	uint32_t overlapped;          /* 1: the next segment was recomputed on a second stream during the adjoint steps */
 	double reverse_ms;            /* device time of the whole reverse sweep (recomputation and adjoint steps) */
 } lbm_adjoint_stats;
