@@ -58,6 +58,20 @@ template<int Q, bool VF> __device__ __forceinline__ void adj_forward(const float
 	s.c3 = -3.0f*fmaf(s.u[0], s.u[0], fmaf(s.u[1], s.u[1], s.u[2]*s.u[2]));
 }
 
+// the same for a TYPE_E cell from its presets (rho_p, u0 = u_p)
+template<int Q, bool VF> __device__ __forceinline__ void adj_from_presets(const float rho_p, const float* u_p, const float* Ft, CellState<Q>& s) {
+	s.rho = rho_p;
+	s.rho2 = 0.5f*v_rcp(rho_p);
+	#pragma unroll
+	for(int d=0; d<3; d++) {
+		s.u0[d] = u_p[d];
+		s.Ft[d] = Ft[d];
+		const float v = VF ? fmaf(Ft[d], s.rho2, s.u0[d]) : s.u0[d];
+		s.kappa[d] = v>-DEF_C && v<DEF_C;
+		s.u[d] = clampc(v);
+	}
+	s.c3 = -3.0f*fmaf(s.u[0], s.u[0], fmaf(s.u[1], s.u[1], s.u[2]*s.u[2]));
+}
 // the same from the fields a forward step collides a fluid cell with: rho and u = clamp(u0 + Ft/(2 rho))
 template<int Q, bool VF> __device__ __forceinline__ void adj_from_fields(const float rho, const float* u, const float* Ft, CellState<Q>& s) {
 	s.rho = rho;
@@ -142,20 +156,20 @@ template<int Q> __device__ __forceinline__ void guo_moments_bar(const CellState<
 // only hbar stays live: pass 1 accumulates rhobar, ubar and Ftbar (Fbar += Ftbar); afterwards
 // gbar_i = (collision part of direction i) + rhobar + c_i.mbar, recomputed per direction and handed
 // to put(integral_constant<int, i>, gbar_i)
-template<int Q, bool TRT, bool VF, class PUT> __device__ __forceinline__ void adj_cell(const CellState<Q>& s, const bool is_e, const float* hbar,
+template<int Q, bool TRT, bool VF, class HB, class PUT> __device__ __forceinline__ void adj_cell(const CellState<Q>& s, const bool is_e, HB&& hbar,
                                                                                      const float ke_weight, const StepArgs& a, float* Fbar, PUT&& put) {
 	float rhobar = 0.0f, ubar[3] = {0.0f, 0.0f, 0.0f}, Ftbar[3] = {0.0f, 0.0f, 0.0f};
 	DirMoments M, S; // moments of w_i feqbar_i and of 9 w_i Gbar_i
 	{
 		float gb, fb, Gb;
-		coll_bar_rest(hbar[0], is_e, TRT, a, gb, fb, Gb);
+		coll_bar_rest(hbar(0), is_e, TRT, a, gb, fb, Gb);
 		acc_moments<0>(M, vs_w<Q>(0)*fb);
 		if constexpr(VF) acc_moments<0>(S, (9.0f*vs_w<Q>(0))*Gb);
 	}
 	Unroll<1, Q, 2>::run([&](auto ic) {
 		constexpr int i = decltype(ic)::value;
 		float gi, gj, fi, fj, Gi, Gj;
-		coll_bar_pair(hbar[i], hbar[i+1], is_e, TRT, a, gi, gj, fi, fj, Gi, Gj);
+		coll_bar_pair(hbar(i), hbar(i+1), is_e, TRT, a, gi, gj, fi, fj, Gi, Gj);
 		const float wi = vs_w<Q>(i); // w_{i+1} = w_i
 		acc_moments<i>(M, wi*fi); acc_moments<i+1>(M, wi*fj);
 		if constexpr(VF) { acc_moments<i>(S, (9.0f*wi)*Gi); acc_moments<i+1>(S, (9.0f*wi)*Gj); }
@@ -192,13 +206,13 @@ template<int Q, bool TRT, bool VF, class PUT> __device__ __forceinline__ void ad
 	};
 	{
 		float gb, fb, Gb;
-		coll_bar_rest(hbar[0], is_e, TRT, a, gb, fb, Gb);
+		coll_bar_rest(hbar(0), is_e, TRT, a, gb, fb, Gb);
 		put(std::integral_constant<int, 0>(), finish(0, 0, 0, gb));
 	}
 	Unroll<1, Q, 2>::run([&](auto ic) {
 		constexpr int i = decltype(ic)::value;
 		float gi, gj, fi, fj, Gi, Gj;
-		coll_bar_pair(hbar[i], hbar[i+1], is_e, TRT, a, gi, gj, fi, fj, Gi, Gj);
+		coll_bar_pair(hbar(i), hbar(i+1), is_e, TRT, a, gi, gj, fi, fj, Gi, Gj);
 		put(std::integral_constant<int, i>(), finish(vs_c(0, i), vs_c(1, i), vs_c(2, i), gi));
 		put(std::integral_constant<int, i+1>(), finish(vs_c(0, i+1), vs_c(1, i+1), vs_c(2, i+1), gj));
 	});
@@ -210,7 +224,10 @@ template<int Q, bool TRT, bool VF, class PUT> __device__ __forceinline__ void ad
 // Slot positions of cell n at the step's parity (32-bit cell indices, N < 2^32): g_0 at n, g_i at
 // A_i = i N + e + n, g_{i+1} at B_i = (i+1) N - e + j_i (e = 0 at odd t, N at even t); the forward
 // store wrote h_i to B_i and h_{i+1} to A_i, so hbar is read there and gbar written to the load positions.
-template<int Q, int ST, bool TRT, int EXT, bool OBJ_ONLY> __global__ void __launch_bounds__(BLOCK, 3) k_adjoint_step(const StepArgs a, const AdjArgs j) {
+#ifndef FX3D_ADJ_MIN_BLOCKS
+#define FX3D_ADJ_MIN_BLOCKS 4 // 64 registers: measured fastest on the C5 sphere channel despite spills (3 blocks: 2.62 ms per reverse step, 4: 2.48)
+#endif
+template<int Q, int ST, bool TRT, int EXT, bool OBJ_ONLY> __global__ void __launch_bounds__(BLOCK, FX3D_ADJ_MIN_BLOCKS) k_adjoint_step(const StepArgs a, const AdjArgs j) {
 	typedef typename Codec<ST>::T T;
 	constexpr bool VF = (EXT&EXT_VF)!=0, FF = (EXT&EXT_FF)!=0, EQ = (EXT&EXT_EQ)!=0;
 	const Grid& g = grid_of(a.g);
@@ -238,21 +255,22 @@ template<int Q, int ST, bool TRT, int EXT, bool OBJ_ONLY> __global__ void __laun
 	const bool is_e = EQ && bo==TYPE_E;
 	const bool ke = j.obj_kind==OBJ_KE_PLANE && j.obj_weight!=0.0f && c.x==j.plane_x && !is_e;
 	if(OBJ_ONLY && !ke) return;
-	float hbar[Q];
+	float hb_[Q];
 	if constexpr(OBJ_ONLY) {
 		#pragma unroll
-		for(int i=0; i<Q; i++) hbar[i] = 0.0f;
+		for(int i=0; i<Q; i++) hb_[i] = 0.0f;
 	} else {
-		hbar[0] = L[n];
-		Unroll<1, Q, 2>::run([&](auto ic) { constexpr int i = decltype(ic)::value; hbar[i] = B(ic); hbar[i+1] = A(i); });
+		hb_[0] = L[n];
+		Unroll<1, Q, 2>::run([&](auto ic) { constexpr int i = decltype(ic)::value; hb_[i] = B(ic); hb_[i+1] = A(i); });
 	}
+	auto hbar = [&](const int i) { return hb_[i]; };
 	CellState<Q> s;
 	{
 		float Ft[3] = {a.fx, a.fy, a.fz};
 		if constexpr(FF) { Ft[0] += a.F[n]; Ft[1] += a.F[N+n]; Ft[2] += a.F[2ull*N+n]; }
 		if(is_e) { // the presets
 			const float up[3] = {a.u[n], a.u[N+n], a.u[2ull*N+n]};
-			adj_forward<Q, VF>(nullptr, true, a.rho[n], up, Ft, s);
+			adj_from_presets<Q, VF>(a.rho[n], up, Ft, s);
 		} else if constexpr(OBJ_ONLY) { // the final state (no step left to write its moments): from its DDFs
 			float gv[Q];
 			load_f32<Q, Codec<ST>>((const T*)j.state, N, st, odd, gv);
