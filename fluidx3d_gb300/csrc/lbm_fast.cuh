@@ -59,6 +59,12 @@ template<> struct RawCodec<ST_FP16C> {
 	}
 };
 
+// The collision of an opposite pair in pair-sum / pair-difference form (see LaneRates) for 16-bit
+// storage, where it saves about a third of the pair's packed instructions and the storage rounding
+// dominates the error; FP32 storage keeps the per-direction form, whose error against the FP64
+// scheme is an order of magnitude lower (the pair-sum form rounds the large parts twice per step).
+template<int ST> __host__ __device__ constexpr bool pair_sum_form() { return ST!=ST_FP32; }
+
 // ---------------------------------------------------------------- one cell (float) or two (float2)
 __device__ __forceinline__ float v_add(const float a, const float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ float v_sub(const float a, const float b) { return __fsub_rn(a, b); }
@@ -128,10 +134,10 @@ template<int C, class V> __device__ __forceinline__ void acc_signed(V& m, bool& 
 }
 
 // S = K*(rho-1) = sum of the shifted DDFs and the momentum (storage units), from pair sums and pair
-// differences; the shift K is added only afterwards (R = S+K), so S keeps full precision. The pair
-// sums and differences replace the pair's DDFs in f (f[i] = f_i + f_j, f[i+1] = f_i - f_j for the
-// opposite pair (i, j = i+1)): the collision works on them directly.
-template<int Q, class V> __device__ __forceinline__ void moments_v(V* f, V& S, V& mx, V& my, V& mz) {
+// differences; the shift K is added only afterwards (R = S+K), so S keeps full precision. SD: the
+// pair sums and differences replace the pair's DDFs in f (f[i] = f_i + f_j, f[i+1] = f_i - f_j for
+// the opposite pair (i, j = i+1)), and the collision works on them directly.
+template<int Q, bool SD, class V> __device__ __forceinline__ void moments_v(V* f, V& S, V& mx, V& my, V& mz) {
 	V s = f[0];
 	bool sx = false, sy = false, sz = false;
 	mx = v_set<V>(0.0f); my = v_set<V>(0.0f); mz = v_set<V>(0.0f);
@@ -140,15 +146,15 @@ template<int Q, class V> __device__ __forceinline__ void moments_v(V* f, V& S, V
 		const V p = v_add(f[i], f[i+1]), d = v_sub(f[i], f[i+1]);
 		s = v_add(s, p);
 		acc_signed<vs_c(0, i)>(mx, sx, d); acc_signed<vs_c(1, i)>(my, sy, d); acc_signed<vs_c(2, i)>(mz, sz, d);
-		f[i] = p; f[i+1] = d;
+		if constexpr(SD) { f[i] = p; f[i+1] = d; }
 	});
 	S = s;
 }
 
 // velocity of the cell(s) (storage-unit DDFs, or the preset rho/u of TYPE_E cells), force shifted and
 // clamped; R = K*rho, Rm1 = K*(rho-1), inv = 1/R. is_e: per-lane TYPE_E flags, any_e: any of them.
-// The opposite pairs of f leave in pair-sum / pair-difference form (moments_v), except for a single
-// TYPE_E cell (float), whose collision does not read f.
+// For 16-bit storage the opposite pairs of f leave in pair-sum / pair-difference form (moments_v),
+// except for a single TYPE_E cell (float), whose collision does not read f.
 template<int Q, int EXT, int ST, class V, class M> __device__ __forceinline__ void cell_rho_u_v(const StepArgs& a, const uint64_t n, V* f, const M is_e,
                                                                                             const bool any_e, V& R, V& Rm1, V& inv, V& ux, V& uy, V& uz,
                                                                                             V& fx, V& fy, V& fz) {
@@ -163,7 +169,7 @@ template<int Q, int EXT, int ST, class V, class M> __device__ __forceinline__ vo
 	};
 	auto from_ddfs = [&]() {
 		V mx, my, mz;
-		moments_v<Q>(f, Rm1, mx, my, mz);
+		moments_v<Q, pair_sum_form<ST>()>(f, Rm1, mx, my, mz);
 		R = v_add(Rm1, v_set<V>(K));
 		inv = v_rcp(R);
 		// u = m/R from the reciprocal plus one Newton correction (u += (m - u R)/R)
@@ -199,7 +205,8 @@ template<int Q, int EXT, int ST, class V, class M> __device__ __forceinline__ vo
 
 // collision rates as values of V: uniform (the host's rates) or per cell (SUBGRID)
 template<class V> struct VRates {
-	V cs, cb, cd, cu, fp, fm; // 1/2 - hp, 2 hp, 1/2 - hm, 2 hm, Guo factors of G_i + G_j and G_i - G_j
+	V w, hp, hm, nhm, half_c_tau, c_taup, c_taum; // per-direction form
+	V cs, cb, cd, cu, fp, fm; // pair-sum form: 1/2 - hp, 2 hp, 1/2 - hm, 2 hm, Guo factors of G_i + G_j and G_i - G_j
 	V rest_rate, rest_force; // the rest direction's relaxation and Guo factors (SRT: w, c_tau; TRT: 2 hp, 2 c_taup)
 };
 // Rates of the pair-sum / pair-difference form of the collision. With S = f_i + f_j, D = f_i - f_j
@@ -208,20 +215,23 @@ template<class V> struct VRates {
 //   f_i' = P + M, f_j' = P - M,  P = (1/2 - hp) S + 2 hp base,  M = (1/2 - hm) D + 2 hm rw uk,
 // and SRT is the case hp = hm = w/2. The Guo terms add c+ (G_i + G_j) to P and c- (G_i - G_j) to M
 // (SRT: c+ = c- = c_tau/2).
-struct LaneRates { float cs, cb, cd, cu, fp, fm, rest_rate, rest_force; };
+struct LaneRates { float w, hp, hm, nhm, half_c_tau, c_taup, c_taum, cs, cb, cd, cu, fp, fm, rest_rate, rest_force; };
 template<bool TRT> __device__ __forceinline__ LaneRates lane_rates(const float w, const float hp, const float hm, const float c_tau, const float c_taup,
                                                                  const float c_taum) {
 	const float hm_ = TRT ? hm : hp; // hp = w/2
-	return LaneRates{__fsub_rn(0.5f, hp), __fadd_rn(hp, hp), __fsub_rn(0.5f, hm_), __fadd_rn(hm_, hm_), TRT ? c_taup : 0.5f*c_tau, TRT ? c_taum : 0.5f*c_tau,
+	return LaneRates{w, hp, hm, -hm, 0.5f*c_tau, c_taup, c_taum,
+	                 __fsub_rn(0.5f, hp), __fadd_rn(hp, hp), __fsub_rn(0.5f, hm_), __fadd_rn(hm_, hm_), TRT ? c_taup : 0.5f*c_tau, TRT ? c_taum : 0.5f*c_tau,
 	                 !TRT ? w : 2.0f*hp, !TRT ? c_tau : 2.0f*c_taup};
 }
 template<class V> __device__ __forceinline__ VRates<V> v_rates(const LaneRates& a);
 template<> __device__ __forceinline__ VRates<float> v_rates<float>(const LaneRates& a) {
-	return VRates<float>{a.cs, a.cb, a.cd, a.cu, a.fp, a.fm, a.rest_rate, a.rest_force};
+	return VRates<float>{a.w, a.hp, a.hm, a.nhm, a.half_c_tau, a.c_taup, a.c_taum, a.cs, a.cb, a.cd, a.cu, a.fp, a.fm, a.rest_rate, a.rest_force};
 }
 __device__ __forceinline__ VRates<float2> v_rates2(const LaneRates& a, const LaneRates& b) {
-	return VRates<float2>{make_float2(a.cs, b.cs), make_float2(a.cb, b.cb), make_float2(a.cd, b.cd), make_float2(a.cu, b.cu),
-	                      make_float2(a.fp, b.fp), make_float2(a.fm, b.fm), make_float2(a.rest_rate, b.rest_rate), make_float2(a.rest_force, b.rest_force)};
+	auto p = [](const float x, const float y) { return make_float2(x, y); };
+	return VRates<float2>{p(a.w, b.w), p(a.hp, b.hp), p(a.hm, b.hm), p(a.nhm, b.nhm), p(a.half_c_tau, b.half_c_tau), p(a.c_taup, b.c_taup),
+	                      p(a.c_taum, b.c_taum), p(a.cs, b.cs), p(a.cb, b.cb), p(a.cd, b.cd), p(a.cu, b.cu), p(a.fp, b.fp), p(a.fm, b.fm),
+	                      p(a.rest_rate, b.rest_rate), p(a.rest_force, b.rest_force)};
 }
 template<> __device__ __forceinline__ VRates<float2> v_rates<float2>(const LaneRates& a) { return v_rates2(a, a); }
 // SUBGRID rates of one cell from its stress tensor H (storage units) and 1/R, with the hardware
@@ -250,8 +260,9 @@ template<int I, class V> __device__ __forceinline__ void stress_add_v(V* H, cons
 	if constexpr(cy!=0 && cz!=0) H[5] = cy*cz>0 ? v_add(H[5], s) : v_sub(H[5], s);
 }
 
-// collision of all directions in place, DDFs in storage units (K scaling), the opposite pairs of f
-// in pair-sum / pair-difference form on entry (moments_v) and as DDFs on exit. EMODE 0: no TYPE_E
+// collision of all directions in place, DDFs in storage units (K scaling); for 16-bit storage the
+// opposite pairs of f are in pair-sum / pair-difference form on entry (moments_v), and f leaves as
+// DDFs in either case. EMODE 0: no TYPE_E
 // cell; 1: the (single) cell is TYPE_E (f = feq, f not read); 2: mixed lanes, TYPE_E lanes picked by
 // is_e. SG: the relaxation rate of each cell from the Smagorinsky-Lilly model
 // (src/kernel.cpp:1579-1593); the stress tensor comes from the pair sums S - (feq_i + feq_j),
@@ -262,6 +273,7 @@ template<int Q, bool TRT, bool VF, int ST, int EMODE, class V, class M, bool SG 
                                                                                                              const V fx, const V fy, const V fz,
                                                                                                              const M is_e, const StepArgs& a) {
 	constexpr float K = RawCodec<ST>::K;
+	constexpr bool SD = pair_sum_form<ST>();
 	const V c3 = v_mul(v_set<V>(-3.0f), v_fma(ux, ux, v_fma(uy, uy, v_mul(uz, uz))));
 	const V ux3 = v_mul(v_set<V>(3.0f), ux), uy3 = v_mul(v_set<V>(3.0f), uy), uz3 = v_mul(v_set<V>(3.0f), uz);
 	V fxK = fx, fyK = fy, fzK = fz, uF = v_set<V>(0.0f); // Guo terms in storage units
@@ -292,7 +304,7 @@ template<int Q, bool TRT, bool VF, int ST, int EMODE, class V, class M, bool SG 
 			constexpr int i = decltype(ic)::value;
 			V uk;
 			const V base = base_of(ic, uk);
-			stress_add_v<i>(H, v_sub(f[i], v_add(base, base)));
+			stress_add_v<i>(H, v_sub(SD ? f[i] : v_add(f[i], f[i+1]), v_add(base, base)));
 		});
 		const float tau0 = __fdiv_rn(1.0f, a.w); // uniform
 		const V inv = v_rcp(R);
@@ -317,7 +329,7 @@ template<int Q, bool TRT, bool VF, int ST, int EMODE, class V, class M, bool SG 
 	}
 	// 2 hm w R per weight class (the factor of uk in M)
 	V cuc[NC];
-	if constexpr(EMODE!=1) {
+	if constexpr(SD && EMODE!=1) {
 		const V cuR = v_mul(r.cu, R);
 		#pragma unroll
 		for(int c=0; c<NC; c++) cuc[c] = v_mul(v_set<V>(vs_w<Q>(c==0 ? 1 : c==1 ? 7 : 19)), cuR);
@@ -331,6 +343,31 @@ template<int Q, bool TRT, bool VF, int ST, int EMODE, class V, class M, bool SG 
 		if constexpr(EMODE==1) { // f = feq = base +- w R uk
 			const V rw = v_mul(v_set<V>(wi), R);
 			f[i] = v_fma(rw, uk, base); f[i+1] = v_fma(v_neg(rw), uk, base);
+		} else if constexpr(!SD) { // per direction: d = feq - f
+			const V rw = v_mul(v_set<V>(wi), R);
+			const V ea = v_fma(rw, uk, base), eb = v_fma(v_neg(rw), uk, base);
+			const V da = v_sub(ea, f[i]), db = v_sub(eb, f[i+1]);
+			V na, nb;
+			if constexpr(!TRT) { na = v_fma(r.w, da, f[i]); nb = v_fma(r.w, db, f[i+1]); }
+			else {
+				const V t = v_mul(r.hp, v_add(da, db)), dd = v_sub(da, db);
+				na = v_add(f[i], v_fma(r.hm, dd, t)); nb = v_add(f[i+1], v_fma(r.nhm, dd, t));
+			}
+			if constexpr(VF) {
+				const V cf = csum_v<i>(fxK, fyK, fzK);
+				const V Y = v_fma(cf, v_mul(uk, v_set<V>(THIRD)), uF);
+				const V gd = v_mul(v_set<V>(6.0f*wi), cf);                     // G_i - G_j
+				if constexpr(!TRT) { // G_i = gs + gd and G_j = gs - gd, each one fused operation
+					na = v_fma(r.half_c_tau, v_fma(v_set<V>(18.0f*wi), Y, gd), na);
+					nb = v_fma(r.half_c_tau, v_fma(v_set<V>(18.0f*wi), Y, v_neg(gd)), nb);
+				} else {
+					const V gs = v_mul(v_set<V>(18.0f*wi), Y);                 // G_i + G_j  (c.u = uk/3)
+					const V m = v_mul(r.c_taum, gd);
+					na = v_add(na, v_fma(r.c_taup, gs, m)); nb = v_add(nb, v_fma(r.c_taup, gs, v_neg(m)));
+				}
+			}
+			if constexpr(EMODE==2) { f[i] = v_pick(na, ea, is_e); f[i+1] = v_pick(nb, eb, is_e); }
+			else { f[i] = na; f[i+1] = nb; }
 		} else {
 			V P = v_fma(r.cs, f[i], v_mul(r.cb, base));
 			V Mn = v_fma(r.cd, f[i+1], v_mul(cuc[c], uk));
