@@ -401,6 +401,9 @@ template<int Q, int ST> __device__ __forceinline__ void read_pair(const typename
 #ifndef FX3D_PIPE_MIN_THREADS
 #define FX3D_PIPE_MIN_THREADS 768 // resident threads per SM the register budget is sized for
 #endif
+#ifndef FX3D_PIPE_MIN_THREADS_SG
+#define FX3D_PIPE_MIN_THREADS_SG 512 // SUBGRID variants (768 spilled and ran at 0.976 ms per step)
+#endif
 #ifndef FX3D_PIPE_STAGES
 #define FX3D_PIPE_STAGES 2
 #endif
@@ -408,10 +411,19 @@ template<int Q, int ST> __device__ __forceinline__ void read_pair(const typename
 #define FX3D_PIPE_Z_CHUNK 2
 #endif
 constexpr int PIPE_STAGES = FX3D_PIPE_STAGES; // pairs in flight per thread: PIPE_STAGES-1 ahead of the one stepped
-inline uint32_t pipe_z_chunk(const GridDesc& g) { return g.Nz<(uint32_t)FX3D_PIPE_Z_CHUNK ? g.Nz : (uint32_t)FX3D_PIPE_Z_CHUNK; } // z planes per thread
+#ifndef FX3D_PIPE_Z_CHUNK_SG
+#define FX3D_PIPE_Z_CHUNK_SG 8
+#endif
+// z planes per thread. The SUBGRID variants run at 2 blocks per SM (124 registers), where the longer
+// walk's prefetch pays: 0.627 ms per step on 512x256x256 FP16S TRT with 8 planes, 0.635 with 4, 0.672
+// with 2.
+template<int EXT> inline uint32_t pipe_z_chunk(const GridDesc& g) {
+	const uint32_t zc = (EXT&EXT_SG)!=0 ? (uint32_t)FX3D_PIPE_Z_CHUNK_SG : (uint32_t)FX3D_PIPE_Z_CHUNK;
+	return g.Nz<zc ? g.Nz : zc;
+}
 template<int Q, int ST> inline size_t pipe_smem(const int stages) { return (size_t)stages*pair_items<Q>()*PIPE_BLOCK*2u*sizeof(typename Codec<ST>::T); }
 
-template<int Q, int ST, bool TRT, int EXT, int S> __global__ void __launch_bounds__(PIPE_BLOCK, ((EXT&EXT_SG)!=0 ? 512 : FX3D_PIPE_MIN_THREADS)/PIPE_BLOCK) k_stream_collide_pairs_pipe(const StepArgs a, const uint32_t zc, const SlotTable tb) {
+template<int Q, int ST, bool TRT, int EXT, int S> __global__ void __launch_bounds__(PIPE_BLOCK, ((EXT&EXT_SG)!=0 ? FX3D_PIPE_MIN_THREADS_SG : FX3D_PIPE_MIN_THREADS)/PIPE_BLOCK) k_stream_collide_pairs_pipe(const StepArgs a, const uint32_t zc, const SlotTable tb) {
 	typedef typename Codec<ST>::T T;
 	typedef typename PairStage<ST>::W SW;
 	constexpr bool EQ = (EXT&EXT_EQ)!=0, VF = (EXT&EXT_VF)!=0;
@@ -706,7 +718,7 @@ template<int ST, int Q, bool TRT, int EXT, bool FAST> inline cudaError_t sc_laun
 					const cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 					if(e!=cudaSuccess) return e;
 				}
-				const uint32_t zc = pipe_z_chunk(a.g);
+				const uint32_t zc = pipe_z_chunk<EXT>(a.g);
 				kernel<<<dim3((a.g.NxNy/2u+PIPE_BLOCK-1u)/PIPE_BLOCK, (a.g.Nz+zc-1u)/zc, 1u), PIPE_BLOCK, smem, s>>>(a, zc, slot_table<typename Codec<ST>::T>(a, Q));
 			}
 		} else {
