@@ -43,7 +43,7 @@ class LBMConfig(ctypes.Structure):
 
 class AdjointConfig(ctypes.Structure):
     _fields_ = [("steps", ctypes.c_uint64), ("checkpoint_interval", ctypes.c_uint64), ("objective", ctypes.c_uint32),
-                ("plane_x", ctypes.c_uint32), ("marker", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
+                ("plane_x", ctypes.c_uint32), ("marker", ctypes.c_uint32), ("workspace_limit_kib", ctypes.c_uint32),
                 ("window_begin", ctypes.c_uint64), ("window_end", ctypes.c_uint64)]
 
 

@@ -747,7 +747,11 @@ extern "C" int lbm_run_adjoint(lbm_domain* d, const lbm_adjoint_config* cfg, dou
 	FX3D_CUDA(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo");
 	const size_t MB = N*16u; // moments of one step
 	const size_t fixed = (size_t)d->cfg.velocity_set*N*4u+N*12u+64u;
-	const size_t margin = 512ull<<20;
+	size_t margin = 512ull<<20;
+	if(cfg->workspace_limit_kib!=0u) { // the caller's cap, within what is free
+		const size_t cap = (size_t)cfg->workspace_limit_kib<<10;
+		if(cap+margin<=free_b) { free_b = cap; margin = 0u; }
+	}
 	uint64_t K2 = K; // steps per (sub-)segment with moments
 	uint32_t levels = 1u;
 	size_t need = (nsnap+1ull)*SB+2ull*K*MB+fixed;

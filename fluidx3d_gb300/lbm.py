@@ -218,18 +218,20 @@ class LBM:
         return np.array(out[:3])
 
     # ------------------------------------------------------------------ adjoint (new; no reference counterpart)
-    def run_adjoint(self, steps, objective="ke_plane", window=None, plane_x=0, marker=TYPE_S, checkpoint_interval=100):
+    def run_adjoint(self, steps, objective="ke_plane", window=None, plane_x=0, marker=TYPE_S, checkpoint_interval=100,
+                    workspace_limit_kib=0):
         """Runs `steps` forward time steps (like run) and the checkpointed discrete adjoint back through
         them. Returns (J, dJ/dF, stats): J the objective averaged over the states after the time steps
         of `window` (inclusive, absolute), dJ/dF as a 3N SoA float32 array. F (the per-cell force field,
-        FORCE_FIELD) is the design variable; the domain ends at the forward state, t advanced by steps."""
+        FORCE_FIELD) is the design variable; the domain ends at the forward state, t advanced by steps.
+        workspace_limit_kib caps the device memory of the adjoint's workspace (0: what is free)."""
         if not self.initialized:
             self.initialize()
         t0 = self.get_t()
         if window is None:
             window = (t0 + steps, t0 + steps)
-        cfg = C.AdjointConfig(int(steps), int(checkpoint_interval), C.OBJECTIVES[objective], int(plane_x), int(marker), 0,
-                              int(window[0]), int(window[1]))
+        cfg = C.AdjointConfig(int(steps), int(checkpoint_interval), C.OBJECTIVES[objective], int(plane_x), int(marker),
+                              int(workspace_limit_kib), int(window[0]), int(window[1]))
         J = ctypes.c_double()
         grad = np.empty(3 * self.get_N(), np.float32)
         st = C.AdjointStats()

@@ -180,7 +180,8 @@ typedef struct lbm_adjoint_config {
 	uint32_t objective;           /* LBM_OBJECTIVE_* */
 	uint32_t plane_x;             /* KINETIC_ENERGY_PLANE_X: plane */
 	uint32_t marker;              /* DRAG_X: flag value of the object's cells */
-	uint32_t reserved;
+	uint32_t workspace_limit_kib; /* at most this much device memory for the adjoint's workspace (KiB; 0: what is free,
+	                               * less a 512 MiB margin); a smaller limit selects a plan with less overlap or two levels */
 	uint64_t window_begin, window_end; /* J is the mean over the states after these time steps (inclusive) */
 } lbm_adjoint_config;
 typedef struct lbm_adjoint_stats {

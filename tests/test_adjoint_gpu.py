@@ -81,3 +81,26 @@ def test_autograd_shim_gives_the_adjoint_gradient(gpu):
     fd = (Jp - Jm) / (2 * h)
     ad = float(np.dot(g2.astype(np.float64), d.astype(np.float64)))
     assert abs(fd - ad) <= 2e-2 * abs(ad), (fd, ad)
+
+
+def test_gpu_adjoint_workspace_plans_give_the_same_gradient(gpu):
+    """A workspace limit selects the plan: two moment sets with overlapped recomputation, one set
+    without overlap, or two levels of DDF sub-snapshots. Every plan recomputes the same states and
+    moments, so J and dJ/dF are bit-identical; too small a limit is an out-of-memory error.
+    Workspace of the 24x12x12 FP32 D3Q19 problem (N = 3456): DDF state 262,656 B, moments of a step
+    55,296 B, lambda + gradient 304,192 B; 40 steps with interval 20: overlapped 3,304,000 B, one set
+    2,198,080 B; interval 40 (one segment): one set 3,041,344 B, two levels (K2 = 7) 2,792,512 B."""
+    from fluidx3d_gb300._capi import LBMError
+    kw = dict(window=(20, 40), plane_x=18)
+    plans = [(20, 0, dict(levels=1, overlapped=1)), (20, 3000, dict(levels=1, overlapped=0)), (40, 2900, dict(levels=2, overlapped=0))]
+    outs = []
+    for interval, limit, expect in plans:
+        with gpu_problem("trt") as lbm:
+            J, g, st = lbm.run_adjoint(40, "ke_plane", checkpoint_interval=interval, workspace_limit_kib=limit, **kw)
+        assert {k: st[k] for k in expect} == expect, (interval, limit, st)
+        outs.append((J, g))
+    for J, g in outs[1:]:
+        assert J == outs[0][0] and np.array_equal(g, outs[0][1])
+    with gpu_problem("trt") as lbm:
+        with pytest.raises(LBMError, match="workspace"):
+            lbm.run_adjoint(40, "ke_plane", checkpoint_interval=20, workspace_limit_kib=1000, **kw)
