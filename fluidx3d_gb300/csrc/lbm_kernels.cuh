@@ -165,7 +165,10 @@ template<int Q, typename T> __device__ __forceinline__ void copy_slots(const T* 
 
 // in place (fi_dst == fi) or out of place (fi_dst != fi: solid and gas cells copy their slots, so
 // dst holds the whole next state)
-template<int Q, int ST, bool TRT, int EXT, bool FAST> __global__ void __launch_bounds__(BLOCK, (Q==19 ? 4 : 2)) k_stream_collide(const StepArgs a) {
+#ifndef FX3D_CELL_MIN_BLOCKS_Q27
+#define FX3D_CELL_MIN_BLOCKS_Q27 3 // D3Q27 one-cell: 1.206 ms per step on 512x256x256 FP32 SRT exact, against 1.421 at 2 blocks (110 registers)
+#endif
+template<int Q, int ST, bool TRT, int EXT, bool FAST> __global__ void __launch_bounds__(BLOCK, (Q==19 ? 4 : FX3D_CELL_MIN_BLOCKS_Q27)) k_stream_collide(const StepArgs a) {
 	typedef typename Codec<ST>::T T;
 	constexpr bool EQ = (EXT&EXT_EQ)!=0;
 	const Grid& g = grid_of(a.g);
@@ -401,6 +404,9 @@ template<int Q, int ST> __device__ __forceinline__ void read_pair(const typename
 #ifndef FX3D_PIPE_MIN_THREADS
 #define FX3D_PIPE_MIN_THREADS 768 // resident threads per SM the register budget is sized for
 #endif
+#ifndef FX3D_PIPE_MIN_THREADS_Q27
+#define FX3D_PIPE_MIN_THREADS_Q27 512 // D3Q27: 768 spilled 120-156 B and ran at 0.977 ms per step on 512x256x256 FP16S SRT, 512 at 0.828
+#endif
 #ifndef FX3D_PIPE_MIN_THREADS_SG
 #define FX3D_PIPE_MIN_THREADS_SG 512 // SUBGRID variants (768 spilled and ran at 0.976 ms per step)
 #endif
@@ -423,7 +429,7 @@ template<int EXT> inline uint32_t pipe_z_chunk(const GridDesc& g) {
 }
 template<int Q, int ST> inline size_t pipe_smem(const int stages) { return (size_t)stages*pair_items<Q>()*PIPE_BLOCK*2u*sizeof(typename Codec<ST>::T); }
 
-template<int Q, int ST, bool TRT, int EXT, int S> __global__ void __launch_bounds__(PIPE_BLOCK, ((EXT&EXT_SG)!=0 ? FX3D_PIPE_MIN_THREADS_SG : FX3D_PIPE_MIN_THREADS)/PIPE_BLOCK) k_stream_collide_pairs_pipe(const StepArgs a, const uint32_t zc, const SlotTable tb) {
+template<int Q, int ST, bool TRT, int EXT, int S> __global__ void __launch_bounds__(PIPE_BLOCK, ((EXT&EXT_SG)!=0 ? FX3D_PIPE_MIN_THREADS_SG : Q==27 ? FX3D_PIPE_MIN_THREADS_Q27 : FX3D_PIPE_MIN_THREADS)/PIPE_BLOCK) k_stream_collide_pairs_pipe(const StepArgs a, const uint32_t zc, const SlotTable tb) {
 	typedef typename Codec<ST>::T T;
 	typedef typename PairStage<ST>::W SW;
 	constexpr bool EQ = (EXT&EXT_EQ)!=0, VF = (EXT&EXT_VF)!=0;
