@@ -227,6 +227,7 @@ def run_gpu_arm(args):
     ms = start.elapsed_time(stop)
     ms_max = max_over_ranks(dist, ms)
     value = world * N * K / (ms_max * 1e-3) / 1e6
+    fluid = int(np.count_nonzero((f["flags"] & 3) != 1))  # cells the step updates (not TYPE_S)
     # ---- end-to-end job through the public API with pinned host buffers
     hb = {k: C.pinned_empty(f[k].shape, f[k].dtype) for k in ("rho", "u", "flags")}
     for k in hb:
@@ -278,6 +279,7 @@ def run_gpu_arm(args):
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d / K, "d2h_bytes_per_step": d2h / K,
                 "job": f"upload rho/u/flags + initialize + {K} steps + update_fields + download rho/u"},
+        "fluid_cells": fluid, "fluid_mlups": world * fluid * K / (ms_max * 1e-3) / 1e6,
         "gpu_launches": K,
         "clocks": clocks.summary(),
     }

@@ -100,8 +100,9 @@ def sphere(storage="fp16s", steps=20000, every=1000, collision="trt", arithmetic
         lbm.u.read_from_device()
         N = lbm.get_N()
         u = lbm.u.data.copy()
+        fluid = int(np.count_nonzero((lbm.flags.data & 3) != 1))
         return dict(run="sphere", storage=storage, collision=collision, steps=steps, drag=drag, mlups=N * steps / (ms * 1e-3) / 1e6,
-                    ux_mean=float(np.mean(u[:N][(lbm.flags.data & 3) == 0]))), u
+                    fluid_mlups=fluid * steps / (ms * 1e-3) / 1e6, ux_mean=float(np.mean(u[:N][(lbm.flags.data & 3) == 0]))), u
 
 
 def large(steps=2000, triangles=200_000, arithmetic="auto"):
@@ -131,7 +132,8 @@ def large(steps=2000, triangles=200_000, arithmetic="auto"):
             lbm.run(steps)
         solid = int(np.count_nonzero((flags & 3) == 1))
         return dict(run="large", cells=lbm.get_N(), triangles=mesh.triangle_number, solid_cells=solid, voxelize_s=t_vox, steps=steps,
-                    mlups=lbm.get_N() * steps / (t.ms * 1e-3) / 1e6, device_bytes_per_cell=lbm.bytes_per_cell_device()), (lbm, mesh)
+                    mlups=lbm.get_N() * steps / (t.ms * 1e-3) / 1e6, fluid_mlups=(lbm.get_N() - solid) * steps / (t.ms * 1e-3) / 1e6,
+                    device_bytes_per_cell=lbm.bytes_per_cell_device()), (lbm, mesh)
     except Exception:
         lbm.close()
         raise
