@@ -524,7 +524,7 @@ template<int Q, int ST, bool TRT, int EXT, int S> __global__ void __launch_bound
 // the bulk loads (cp.async.bulk, completion on the stage's mbarrier) of x-rows j+1..j+P are in flight
 // and the bulk stores of x-row j-1 drain. Every global access is a whole 16-byte-aligned row and no
 // data in flight occupies registers. Slots of solid cells go back unchanged, so the step may also
-// write to a different array than it reads (fi_dst), which the adjoint's recomputation uses.
+// write to a different array than it reads (fi_dst).
 struct RowStageLayout {
 	uint32_t rowbytes, stride, flags_off, stage_bytes;
 	__host__ __device__ RowStageLayout(const int q, const uint32_t elem, const uint32_t Nx) {
