@@ -10,20 +10,21 @@ from test_adjoint_oracle import channel_problem
 pytestmark = pytest.mark.gpu
 
 
-def gpu_problem(collision, storage="fp32", Nx=24, Ny=12, Nz=12, seed=3):
+def gpu_problem(collision, storage="fp32", Nx=24, Ny=12, Nz=12, seed=3, q=19):
     f = S.sphere_channel(Nx, Ny, Nz, u_in=0.05, radius=2.5, center=(8.0, 6.0, 6.0))
     F = S.box_filter_noise(Nx, Ny, Nz, sigma=1e-4, width=3, seed=seed)
-    lbm = LBM(Nx, Ny, Nz, 0.02, 2e-6, 0.0, 0.0, collision=collision, storage=storage, extensions=("eq", "ff", "vf"))
+    lbm = LBM(Nx, Ny, Nz, 0.02, 2e-6, 0.0, 0.0, velocity_set=q, collision=collision, storage=storage, extensions=("eq", "ff", "vf"))
     lbm.rho.data[:], lbm.u.data[:], lbm.flags.data[:], lbm.F.data[:] = f["rho"], f["u"], f["flags"], F
     return lbm
 
 
-@pytest.mark.parametrize("collision,kind", [("srt", "ke_plane"), ("trt", "ke_plane"), ("trt", "drag_x"), ("srt", "drag_x")])
-def test_gpu_adjoint_matches_fp64_adjoint(collision, kind, gpu):
-    o, f0 = channel_problem(collision)
+@pytest.mark.parametrize("collision,kind,q", [("srt", "ke_plane", 19), ("trt", "ke_plane", 19), ("trt", "drag_x", 19), ("srt", "drag_x", 19),
+                                              ("trt", "ke_plane", 27), ("srt", "drag_x", 27)])
+def test_gpu_adjoint_matches_fp64_adjoint(collision, kind, q, gpu):
+    o, f0 = channel_problem(collision, q=q)
     obj = oracle.objective(kind, 28, 40, plane_x=18, marker=0x41)
     J64, g64 = oracle.fp64_adjoint(o, f0, 40, obj, interval=7, force=(2e-6, 0.0, 0.0))
-    with gpu_problem(collision) as lbm:
+    with gpu_problem(collision, q=q) as lbm:
         J, g, stats = lbm.run_adjoint(40, kind, window=(28, 40), plane_x=18, marker=0x41, checkpoint_interval=7)
         assert lbm.get_t() == 40
     assert J == pytest.approx(J64, rel=2e-5)

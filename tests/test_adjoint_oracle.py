@@ -7,18 +7,18 @@ import oracle
 from fluidx3d_gb300 import setups as S
 
 
-def channel_problem(collision, Nx=24, Ny=12, Nz=12, seed=3):
+def channel_problem(collision, Nx=24, Ny=12, Nz=12, seed=3, q=19):
     f = S.sphere_channel(Nx, Ny, Nz, u_in=0.05, radius=2.5, center=(8.0, 6.0, 6.0))
     F = S.box_filter_noise(Nx, Ny, Nz, sigma=1e-4, width=3, seed=seed)
-    o = oracle.Oracle(Nx, Ny, Nz, q=19, collision=collision, extensions=("eq", "ff", "vf"), nu=0.02, precision="f64")
+    o = oracle.Oracle(Nx, Ny, Nz, q=q, collision=collision, extensions=("eq", "ff", "vf"), nu=0.02, precision="f64")
     o.rho[:], o.u[:], o.flags[:], o.F[:] = f["rho"], f["u"], f["flags"], F
     o.initialize()
     return o, o.fi.copy()
 
 
-@pytest.mark.parametrize("collision,kind", [("srt", "ke_plane"), ("trt", "ke_plane"), ("trt", "drag_x")])
-def test_fp64_adjoint_matches_central_differences(collision, kind):
-    o, f0 = channel_problem(collision)
+@pytest.mark.parametrize("collision,kind,q", [("srt", "ke_plane", 19), ("trt", "ke_plane", 19), ("trt", "drag_x", 19), ("trt", "ke_plane", 27)])
+def test_fp64_adjoint_matches_central_differences(collision, kind, q):
+    o, f0 = channel_problem(collision, q=q)
     steps = 40
     obj = oracle.objective(kind, 28, 40, plane_x=18, marker=0x41)
     force = (2e-6, 0.0, 0.0)
