@@ -781,7 +781,12 @@ extern "C" int lbm_run_adjoint(lbm_domain* d, const lbm_adjoint_config* cfg, dou
 	auto in_window = [&](const uint64_t t) { return t>=cfg->window_begin && t<=cfg->window_end; };
 	auto args_at = [&](const uint64_t t, const void* state) { StepArgs a = d->args(); a.t = t; a.fi = const_cast<void*>(state); return a; };
 
-	// ---- forward sweep (in place on the domain's DDFs), snapshots, objective
+	// ---- forward sweep (in place on the domain's DDFs), snapshots, objective. With one level, the
+	// steps of the last segment write its moment checkpoints themselves (the same kernel on the same
+	// states as a recomputation), so the reverse sweep starts without recomputing it; not when the
+	// domain's steps already write their fields to rho/u (UPDATE_FIELDS)
+	const uint64_t last0 = (nsnap-1ull)*K, last_set = overlap ? ((nsnap-1ull)&1ull) : 0ull;
+	const bool forward_moments = levels==1u && !d->fused_fields;
 	FX3D_CUDA(cudaMemsetAsync(Jd.p, 0, sizeof(double), d->stream), "cudaMemsetAsync(J)");
 	EventTimer tf(d->stream);
 	for(uint64_t k=0ull; k<=T; k++) {
@@ -790,7 +795,11 @@ extern "C" int lbm_run_adjoint(lbm_domain* d, const lbm_adjoint_config* cfg, dou
 			j.state = d->fi; j.obj_weight = (float)weight;
 			FX3D_CUDA(launch_objective_value(d->v, args_at(t0+k, d->fi), j, d->partials, (double*)Jd.p, d->stream), "objective");
 		}
-		if(k<T) { const int r = launch_stream_collide(d); if(r!=LBM_OK) return r; d->t++; }
+		if(k<T) {
+			const int r = forward_moments && k>=last0 ? step_with_moments(d, d->fi, mom(last_set, k-last0), t0+k, d->stream) : launch_stream_collide(d);
+			if(r!=LBM_OK) return r;
+			d->t++;
+		}
 	}
 	const double forward_ms = tf.stop(d->stream);
 	// ---- reverse sweep
@@ -826,7 +835,7 @@ extern "C" int lbm_run_adjoint(lbm_domain* d, const lbm_adjoint_config* cfg, dou
 		auto recompute_segment = [&](const uint64_t sg, const bool wait_set) -> int {
 			const uint64_t k0 = sg*K, k1 = std::min<uint64_t>(k0+K, T);
 			if(wait_set) FX3D_CUDA(cudaStreamWaitEvent(ov.stream, adj_done[sg&1ull], 0), "cudaStreamWaitEvent");
-			{ const int r = recompute(k0, k1, snap(sg), sg&1ull, ov.stream); if(r!=LBM_OK) return r; }
+			if(!(forward_moments && sg==nsnap-1ull)) { const int r = recompute(k0, k1, snap(sg), sg&1ull, ov.stream); if(r!=LBM_OK) return r; }
 			FX3D_CUDA(cudaEventRecord(rec_done[sg&1ull], ov.stream), "cudaEventRecord");
 			return LBM_OK;
 		};
@@ -856,7 +865,7 @@ extern "C" int lbm_run_adjoint(lbm_domain* d, const lbm_adjoint_config* cfg, dou
 		for(uint64_t b=nb; b-->0ull;) {
 			const uint64_t b0 = levels==2u ? k0+b*K2 : k0, b1 = levels==2u ? std::min<uint64_t>(k0+(b+1ull)*K2, k1) : k1;
 			EventTimer tr(d->stream);
-			{ const int r = recompute(b0, b1, levels==2u ? subs(b) : snap(s), 0ull, d->stream); if(r!=LBM_OK) return r; }
+			if(!(forward_moments && s==nsnap-1ull)) { const int r = recompute(b0, b1, levels==2u ? subs(b) : snap(s), 0ull, d->stream); if(r!=LBM_OK) return r; }
 			recompute_ms += tr.stop(d->stream);
 			EventTimer ta(d->stream);
 			{ const int r = adjoint_steps(b0, b1, 0ull); if(r!=LBM_OK) return r; }
